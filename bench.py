@@ -1,0 +1,315 @@
+"""Throughput of the relaxing-TVD split MHD step on GB300.
+
+One "step" is one full Strang step x(F,A) T12 y(F,A) T13 z(F,A,A,F) T13 y(A,F)
+T12 x(A,F) (C/mhd.c:59-124) of the 256^3 decaying-turbulence box (FP32,
+gamma 5/3, CFL 0.7, seeded k^-2 velocity at rms Mach 0.5, B = 0.3 x + dB).
+Metric: cell-updates/s = 256^3 * steps / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--size N] [--variant plain|fused]
+
+Our arm prints one JSON line with:
+  value       device throughput, state resident in HBM, timed with CUDA events
+              on the library's stream (max over ranks);
+  e2e         the same metric through the C ABI with host buffers: every step
+              copies the state in from pinned host memory and back out;
+  roofline    the dominant kernel's algorithmic bytes per launch over its mean
+              launch time (events around every launch in the timed region),
+              against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (the reference's C path) on this host's cores;
+  clocks      nvidia-smi samples taken during the timed region.
+The state (537 MB at 256^3) is larger than L2 (126 MB), so no L2 flush is
+needed between steps.  With --gpus N > 1 (torchrun) every rank advances its
+own box: replicas with no collective ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# algorithmic HBM bytes per cell for one launch of each kernel (FP32 AoS:
+# u 20 B, b 12 B per cell)
+ALG_BYTES = {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 64, "calcfl": 32, "copy": 64,
+             "cfl_finalize": 0, "sweep": 64}
+STEP_BYTES = {"plain": 864, "fused": 320}
+METRIC = "cell-updates/s at 256^3 (plain vs fused); closure speedup at matched error"
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_baseline(size: int, seconds: float = 12.0):
+    """The oracle (the reference's C arithmetic) on this host's cores."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _oracle import REF, Oracle, strang_by_ops  # the checker, timed as the CPU baseline
+
+    import heterogeneous_mhd_gb300 as mhd
+
+    u, b = mhd.init_turbulence(size, seed=0)
+    port = Oracle(32, "port")
+    cores = port.max_threads()
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        u, b, _, _, _ = port.strang(u, b, size, size, size, 1)
+        steps += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": size ** 3 * steps / el, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} full Strang steps of the {size}^3 turbulence box, oracle restatement of the "
+                      f"reference C path with OpenMP over pencils ({cores} threads)"}
+
+
+def reference_arm(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _oracle import REF, Oracle, strang_by_ops
+
+    import heterogeneous_mhd_gb300 as mhd
+
+    n = args.size
+    u, b = mhd.init_turbulence(n, seed=0)
+    kind, o = "port", Oracle(32, "port")
+    cores = o.max_threads()
+    for _ in range(args.warmup):
+        u, b, _, _, _ = o.strang(u, b, n, n, n, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u, b, _, _, _ = o.strang(u, b, n, n, n, 1)
+    el = time.perf_counter() - t0
+    v = n ** 3 * args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": f"decaying turbulence {n}^3, FP32, CFL 0.7, plain Strang step",
+                                            "grid": [n, n, n], "cpu": True},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": kind,
+                             "sample": f"full {n}^3 Strang steps; the reference's C/ arithmetic restated in "
+                                       f"oracle/mhd_oracle.c (bit-identical to the reference build), OpenMP over "
+                                       f"pencils, {cores} threads"},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def our_arm(args):
+    import torch
+
+    import heterogeneous_mhd_gb300 as mhd
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = args.size
+    cells = n ** 3
+    u0, b0 = mhd.init_turbulence(n, seed=rank)
+    ctx = mhd.Context(n, n, n)
+    ctx.set_state(u0, b0)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    fused = args.variant == "fused"
+
+    def barrier():
+        ctx.sync()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up (also captures the step graph)
+    ctx.step(args.warmup, cfl=0.7, fused=fused)
+    barrier()
+
+    # timed region: per-kernel events around every launch (direct launches)
+    ctx.profile(True)
+    ctx.profile_reset()
+    l0 = ctx.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier()
+        ev0.record(stream)
+        ctx.step(args.steps, cfl=0.7, fused=fused)
+        ev1.record(stream)
+        ev1.synchronize()
+        barrier()
+    launches = ctx.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    kern = {k: ctx.profile_read(k) for k in mhd.KERNELS}
+    ctx.profile(False)
+    status = ctx.check()
+
+    # same steps as graph replays (production path), for reference
+    barrier()
+    ev0.record(stream)
+    ctx.step(args.steps, cfl=0.7, fused=fused)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms_graph = ev0.elapsed_time(ev1)
+
+    t_max = ms
+    if dist is not None:
+        tt = torch.tensor([ms, ms_graph], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max, ms_graph = float(tt[0]), float(tt[1])
+    value = world * cells * args.steps / (t_max * 1e-3)
+
+    # e2e: host state in and out of the C ABI every step
+    hu = torch.empty(5 * cells, dtype=torch.float32, pin_memory=True)
+    hb = torch.empty(3 * cells, dtype=torch.float32, pin_memory=True)
+    hu.numpy()[:] = u0
+    hb.numpy()[:] = b0
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.set_state(hu, hb)   # H2D from pinned memory
+        ctx.step(1, cfl=0.7, fused=fused)
+        ctx.get_state_into(hu, hb)  # D2H, synchronises
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt[0])
+    e2e = world * cells * e2e_steps / e2e_s
+
+    # roofline of the dominant kernel
+    hbm, src = peaks()
+    dom = max((k for k in kern if kern[k][1] > 0), key=lambda k: kern[k][0])
+    tot_ms, nl = kern[dom]
+    mean_ms = tot_ms / nl
+    achieved = ALG_BYTES[dom] * cells / (mean_ms * 1e-3) / 1e9
+    step_bw = STEP_BYTES[args.variant] * cells / (ms / args.steps * 1e-3) / 1e9
+    if rank != 0:
+        ctx.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    share = {k: round(v[0] / sum(x[0] for x in kern.values()), 4) for k, v in kern.items() if v[1] > 0}
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"decaying turbulence {n}^3, FP32, CFL 0.7, {args.variant} Strang step",
+                   "grid": [n, n, n], "variant": args.variant, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "state 537 MB > L2, no flush"},
+        "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": 32 * cells,
+                "d2h_bytes_per_step": 32 * cells, "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": src, "traffic": None,
+                     "alg_bytes_per_launch": ALG_BYTES[dom] * cells, "mean_launch_ms": mean_ms,
+                     "step_alg_gbs": step_bw, "step_frac": step_bw / hbm},
+        "kernels": {k: {"ms_total": round(v[0], 4), "launches": v[1], "share": share.get(k, 0.0)}
+                    for k, v in kern.items() if v[1] > 0},
+        "graph_ms_per_step": ms_graph / args.steps,
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "status": int(status),
+    }
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(n)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--variant", default="plain", choices=["plain", "fused"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1052 @@
+// C ABI of mhd_gb300 (include/mhd_gb300.h): the drop-in functions with the
+// reference's names (C/spu_function.h:1-15), the context API, the Strang step
+// driver (C/mhd.c:59-124) and its CUDA-graph capture.  Host code only; every
+// computation runs in the kernels of mhd_kernels.cuh.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mhd_gb300.h"
+#include "mhd_launch.h"
+
+using namespace mhd;
+
+// ----------------------------------------------------------------- status
+
+static thread_local int g_last_error = MHD_OK;
+
+static int set_err(int e)
+{
+    g_last_error = e;
+    return e;
+}
+
+#define CUDA_TRY(call)                                                                    \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            if (getenv("MHD_GB300_DEBUG"))                                                \
+                fprintf(stderr, "mhd_gb300: %s failed: %s (%s:%d)\n", #call,              \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                      \
+            return (e_ == cudaErrorMemoryAllocation) ? MHD_ERR_NOMEM : MHD_ERR_CUDA;     \
+        }                                                                                 \
+    } while (0)
+
+#define MHD_TRY(call)                  \
+    do {                               \
+        int s_ = (call);               \
+        if (s_ != MHD_OK)              \
+            return s_;                 \
+    } while (0)
+
+extern "C" MHD_API int mhd_last_error(void) { return g_last_error; }
+
+extern "C" MHD_API const char* mhd_error_string(int status)
+{
+    switch (status) {
+    case MHD_OK: return "ok";
+    case MHD_ERR_ARG: return "bad argument";
+    case MHD_ERR_CUDA: return "CUDA runtime error";
+    case MHD_ERR_TIMEOUT: return "device-side wait timed out";
+    case MHD_ERR_NONFINITE: return "non-finite value in the CFL reduction";
+    case MHD_ERR_UNSUPPORTED: return "unsupported shape or mode";
+    case MHD_ERR_NOMEM: return "device allocation failed";
+    default: return "unknown status";
+    }
+}
+
+// ---------------------------------------------------------------- context
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= cap)
+            return MHD_OK;
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (bytes == 0)
+            return MHD_OK;
+        CUDA_TRY(cudaMalloc(&p, bytes));
+        cap = bytes;
+        return MHD_OK;
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct Pending {
+    int kernel;
+    cudaEvent_t a, b;
+};
+
+struct mhd_ctx {
+    int nx, ny, nz, flags;
+    const KernelSet* ks;
+    int elem;
+    int device;
+    cudaStream_t stream = nullptr;
+    DevBuf U[2], B[2];  // ping-pong state; the current state is (U[0], B[0])
+    DevBuf part;        // CFL partials
+    DevBuf clock;       // R[4]: t, tf, dt, 1/c
+    DevBuf misc;        // err (int) + nsteps (long long) + divb partial scratch
+    DevBuf stage[4];    // drop-in host staging
+    DevBuf alias[2];    // private copies of inputs that alias an output
+    DevBuf divb;
+    int* err_dev = nullptr;
+    long long* nsteps_dev = nullptr;
+    bool have_state = false;
+    bool cfl_valid = false;  // part holds the CFL partials of the current state
+    int cfl_nparts = 0;
+    // graphs, one per step variant
+    int use_graphs = 1;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    double gcfl[2] = {0, 0};
+    int glaunches[2] = {0, 0};
+    bool capturing = false;
+    // profiling
+    int profile = 0;
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> ev_free;
+    double total_ms[MHD_K_COUNT] = {0};
+    long long nlaunch[MHD_K_COUNT] = {0};
+    long long launch_count = 0;
+};
+
+static size_t ncell(const mhd_ctx* c) { return (size_t)c->nx * c->ny * c->nz; }
+
+static cudaEvent_t ev_get(mhd_ctx* c)
+{
+    if (!c->ev_free.empty()) {
+        cudaEvent_t e = c->ev_free.back();
+        c->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets one kernel launch with events when profiling (never while capturing).
+struct KTimer {
+    mhd_ctx* c;
+    int id;
+    cudaEvent_t a = nullptr, b = nullptr;
+    KTimer(mhd_ctx* ctx, int kid) : c(ctx), id(kid)
+    {
+        c->launch_count++;
+        if (c->profile && !c->capturing) {
+            a = ev_get(c);
+            b = ev_get(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~KTimer()
+    {
+        if (a) {
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({id, a, b});
+        }
+    }
+};
+
+static void drain_profile(mhd_ctx* c)
+{
+    if (c->pending.empty())
+        return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& p : c->pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            c->total_ms[p.kernel] += ms;
+            c->nlaunch[p.kernel] += 1;
+        }
+        c->ev_free.push_back(p.a);
+        c->ev_free.push_back(p.b);
+    }
+    c->pending.clear();
+}
+
+static const KernelSet* pick_set(int flags)
+{
+    const bool f64 = (flags & MHD_F64) != 0;
+    const bool ex = (flags & MHD_MODE_EXACT) != 0;
+    if (f64)
+        return kernels_f64_exact();  // the FP64 build follows the reference's order
+    return ex ? kernels_f32_exact() : kernels_f32_fast();
+}
+
+static int check_dims(int nx, int ny, int nz)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0)
+        return MHD_ERR_ARG;
+    if (nx > 512 || ny > 65535 * 64 || nz > 65535)
+        return MHD_ERR_UNSUPPORTED;
+    return MHD_OK;
+}
+
+static void invalidate_graphs(mhd_ctx* c)
+{
+    for (int v = 0; v < 2; v++)
+        if (c->gexec[v]) {
+            cudaGraphExecDestroy(c->gexec[v]);
+            c->gexec[v] = nullptr;
+        }
+}
+
+extern "C" MHD_API int mhd_create(mhd_ctx** out, int nx, int ny, int nz, int flags)
+{
+    if (!out || nx <= 0 || ny <= 0 || nz <= 0)
+        return set_err(MHD_ERR_ARG);
+    *out = nullptr;
+    mhd_ctx* c = new mhd_ctx();
+    c->nx = nx;
+    c->ny = ny;
+    c->nz = nz;
+    c->flags = flags;
+    c->ks = pick_set(flags);
+    c->elem = c->ks->elem;
+    if (cudaGetDevice(&c->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return set_err(MHD_ERR_CUDA);
+    }
+    int s = c->clock.ensure(4 * sizeof(double));
+    if (s == MHD_OK)
+        s = c->misc.ensure(64);
+    if (s != MHD_OK) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return set_err(s);
+    }
+    c->err_dev = static_cast<int*>(c->misc.p);
+    c->nsteps_dev = reinterpret_cast<long long*>(static_cast<char*>(c->misc.p) + 8);
+    cudaMemsetAsync(c->misc.p, 0, 64, c->stream);
+    // clock: t = 0, tf = +inf
+    if (c->elem == 4) {
+        float h[4] = {0.f, INFINITY, 0.f, 0.f};
+        cudaMemcpyAsync(c->clock.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream);
+    } else {
+        double h[4] = {0.0, INFINITY, 0.0, 0.0};
+        cudaMemcpyAsync(c->clock.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream);
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return set_err(MHD_ERR_CUDA);
+    }
+    *out = c;
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_destroy(mhd_ctx* c)
+{
+    if (!c)
+        return MHD_ERR_ARG;
+    cudaStreamSynchronize(c->stream);
+    drain_profile(c);
+    invalidate_graphs(c);
+    for (auto& e : c->ev_free)
+        cudaEventDestroy(e);
+    for (int v = 0; v < 2; v++) {
+        c->U[v].release();
+        c->B[v].release();
+    }
+    c->part.release();
+    c->clock.release();
+    c->misc.release();
+    c->divb.release();
+    for (auto& s : c->stage)
+        s.release();
+    for (auto& s : c->alias)
+        s.release();
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return MHD_OK;
+}
+
+extern "C" MHD_API void* mhd_stream(mhd_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" MHD_API int mhd_sync(mhd_ctx* c)
+{
+    if (!c)
+        return MHD_ERR_ARG;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MHD_OK;
+}
+
+// ------------------------------------------------------------ operators
+
+static int op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx, int ny, int nz, double dt,
+                     const void* dt_dev, void* cfl_part)
+{
+    MHD_TRY(check_dims(nx, ny, nz));
+    FluidxArgs a{};
+    a.u_out = u;
+    a.uu = uu;
+    a.ub = ub;
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.P = fluidx_pencils(nx, ny);
+    const uintptr_t al = reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(uu) |
+                         reinterpret_cast<uintptr_t>(ub);
+    a.use_tma = ((al & 15) == 0) && ((size_t)nx * 5 * c->elem) % 16 == 0 && ((size_t)nx * 3 * c->elem) % 16 == 0;
+    a.dt_val = dt;
+    a.dt_ptr = dt_dev;
+    a.cfl_part = cfl_part;
+    a.err = c->err_dev;
+    KTimer kt(c, MHD_K_FLUIDX);
+    CUDA_TRY(c->ks->fluidx(a, c->stream));
+    return MHD_OK;
+}
+
+static int op_advect(mhd_ctx* c, void* b_out, const void* b1_src, const void* uu, const void* ub, int nx, int ny,
+                     int nz, double dt, const void* dt_dev)
+{
+    MHD_TRY(check_dims(nx, ny, nz));
+    AdvectArgs a{};
+    a.b_out = b_out;
+    a.b1_src = b1_src;
+    a.uu = uu;
+    a.ub = ub;
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.P = advect_pencils(nx, ny);
+    a.dt_val = dt;
+    a.dt_ptr = dt_dev;
+    a.err = c->err_dev;
+    KTimer kt(c, MHD_K_ADVECT);
+    CUDA_TRY(c->ks->advect(a, c->stream));
+    return MHD_OK;
+}
+
+static int op_transpose(mhd_ctx* c, int axis, void* u, void* b, const void* uu, const void* ub, int nx, int ny,
+                        int nz)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0)
+        return MHD_ERR_ARG;
+    if (axis == 2 && nx != nz)
+        return MHD_ERR_ARG;
+    TransposeArgs a{u, b, uu, ub, nx, ny, nz, axis};
+    KTimer kt(c, axis == 1 ? MHD_K_TRANSPOSE12 : MHD_K_TRANSPOSE13);
+    CUDA_TRY(c->ks->transpose(a, c->stream));
+    return MHD_OK;
+}
+
+static int op_copy(mhd_ctx* c, const void* src, void* dst, size_t bytes)
+{
+    if (src == dst || bytes == 0)
+        return MHD_OK;
+    KTimer kt(c, MHD_K_COPY);
+    CUDA_TRY(launch_copy(src, dst, bytes, c->stream));
+    return MHD_OK;
+}
+
+// First CFL pass into c->part; returns the partial count in *np.
+static int op_calcfl_partials(mhd_ctx* c, const void* u, const void* b, size_t cells, int* np)
+{
+    MHD_TRY(c->part.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
+    KTimer kt(c, MHD_K_CALCFL);
+    CUDA_TRY(c->ks->calcfl(u, b, cells, c->part.p, np, c->stream));
+    return MHD_OK;
+}
+
+static int op_finalize(mhd_ctx* c, int nparts, const void* u, const void* b, int nx, int ny, int nz, double cfl,
+                       int advance)
+{
+    CflFinalizeArgs a{};
+    a.part = c->part.p;
+    a.nparts = nparts;
+    a.u = u;
+    a.b = b;
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.cfl = cfl;
+    a.advance = advance;
+    a.clock = c->clock.p;
+    a.nsteps = c->nsteps_dev;
+    a.err = c->err_dev;
+    KTimer kt(c, MHD_K_FINALIZE);
+    CUDA_TRY(c->ks->cfl_finalize(a, c->stream));
+    return MHD_OK;
+}
+
+extern "C" MHD_API int mhd_op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx, int ny, int nz,
+                                     double dt)
+{
+    if (!c || !u || !uu || !ub)
+        return set_err(MHD_ERR_ARG);
+    return set_err(op_fluidx(c, u, uu, ub, nx, ny, nz, dt, nullptr, nullptr));
+}
+
+extern "C" MHD_API int mhd_op_advectbyzx(mhd_ctx* c, void* b, const void* uu, const void* ub, int nx, int ny,
+                                         int nz, double dt)
+{
+    if (!c || !b || !uu || !ub)
+        return set_err(MHD_ERR_ARG);
+    const void* src = ub;
+    if (b == ub) {  // the fused kernel reads neighbour rows of update_b: keep a private copy
+        const size_t bytes = (size_t)nx * ny * nz * 3 * c->elem;
+        MHD_TRY(set_err(c->alias[1].ensure(bytes)));
+        MHD_TRY(set_err(op_copy(c, ub, c->alias[1].p, bytes)));
+        src = c->alias[1].p;
+    }
+    return set_err(op_advect(c, b, b, uu, src, nx, ny, nz, dt, nullptr));
+}
+
+static int transpose_entry(mhd_ctx* c, int axis, void* u, void* b, const void* uu, const void* ub, int nx, int ny,
+                           int nz)
+{
+    if (!c || !u || !b || !uu || !ub)
+        return MHD_ERR_ARG;
+    if (axis == 2 && nx != nz)
+        return MHD_ERR_ARG;
+    const size_t cells = (size_t)nx * ny * nz;
+    if (u == uu) {
+        MHD_TRY(c->alias[0].ensure(cells * 5 * c->elem));
+        MHD_TRY(op_copy(c, uu, c->alias[0].p, cells * 5 * c->elem));
+        uu = c->alias[0].p;
+    }
+    if (b == ub) {
+        MHD_TRY(c->alias[1].ensure(cells * 3 * c->elem));
+        MHD_TRY(op_copy(c, ub, c->alias[1].p, cells * 3 * c->elem));
+        ub = c->alias[1].p;
+    }
+    return op_transpose(c, axis, u, b, uu, ub, nx, ny, nz);
+}
+
+extern "C" MHD_API int mhd_op_transpose12(mhd_ctx* c, void* u, void* b, const void* uu, const void* ub, int nx,
+                                          int ny, int nz)
+{
+    return set_err(transpose_entry(c, 1, u, b, uu, ub, nx, ny, nz));
+}
+
+extern "C" MHD_API int mhd_op_transpose13(mhd_ctx* c, void* u, void* b, const void* uu, const void* ub, int nx,
+                                          int ny, int nz)
+{
+    return set_err(transpose_entry(c, 2, u, b, uu, ub, nx, ny, nz));
+}
+
+extern "C" MHD_API int mhd_op_copy(mhd_ctx* c, const void* u, const void* b, void* uu, void* ub, int nx, int ny,
+                                   int nz)
+{
+    if (!c || !u || !b || !uu || !ub || nx < 0 || ny < 0 || nz < 0)
+        return set_err(MHD_ERR_ARG);
+    const size_t cells = (size_t)nx * ny * nz;
+    MHD_TRY(set_err(op_copy(c, u, uu, cells * 5 * c->elem)));
+    return set_err(op_copy(c, b, ub, cells * 3 * c->elem));
+}
+
+static int read_clock(mhd_ctx* c, double out[4])
+{
+    if (c->elem == 4) {
+        float h[4];
+        CUDA_TRY(cudaMemcpyAsync(h, c->clock.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        for (int s = 0; s < 4; s++)
+            out[s] = h[s];
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(out, c->clock.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    return MHD_OK;
+}
+
+static int calcfl_sync(mhd_ctx* c, const void* u, const void* b, int nx, int ny, int nz, double* inv)
+{
+    const size_t cells = (size_t)nx * ny * nz;
+    if (cells == 0) {  // the reference returns 1/0 with c = 0
+        *inv = INFINITY;
+        return MHD_OK;
+    }
+    int np = 0;
+    MHD_TRY(op_calcfl_partials(c, u, b, cells, &np));
+    MHD_TRY(op_finalize(c, np, u, b, nx, ny, nz, 0.0, 0));
+    double clk[4];
+    MHD_TRY(read_clock(c, clk));
+    *inv = clk[3];
+    int herr = 0;
+    CUDA_TRY(cudaMemcpy(&herr, c->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr & DEVERR_NONFINITE) {
+        CUDA_TRY(cudaMemsetAsync(c->err_dev, 0, sizeof(int), c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        return MHD_ERR_NONFINITE;
+    }
+    return MHD_OK;
+}
+
+extern "C" MHD_API int mhd_op_calcfl(mhd_ctx* c, const void* u, const void* b, int nx, int ny, int nz,
+                                     double* inv_cmax)
+{
+    if (!c || !u || !b || !inv_cmax || nx < 0 || ny < 0 || nz < 0)
+        return set_err(MHD_ERR_ARG);
+    return set_err(calcfl_sync(c, u, b, nx, ny, nz, inv_cmax));
+}
+
+// ----------------------------------------------------------------- state
+
+extern "C" MHD_API int mhd_set_state(mhd_ctx* c, const void* u, const void* b, int where)
+{
+    if (!c || !u || !b)
+        return set_err(MHD_ERR_ARG);
+    const size_t bu = ncell(c) * 5 * c->elem, bb = ncell(c) * 3 * c->elem;
+    for (int v = 0; v < 2; v++) {
+        MHD_TRY(set_err(c->U[v].ensure(bu)));
+        MHD_TRY(set_err(c->B[v].ensure(bb)));
+    }
+    // CFL partials for both producers (standalone calcfl and the fluidx
+    // epilogue), allocated here so a captured step never reallocates.
+    {
+        const size_t a = (ncell(c) + 255) / 256;
+        const size_t f = (size_t)(c->ny / fluidx_pencils(c->nx, c->ny)) * c->nz;
+        MHD_TRY(set_err(c->part.ensure(((a > f ? a : f) + 1) * c->ks->part_bytes)));
+    }
+    (void)where;  // direction inferred from the pointers (unified addressing)
+    const cudaMemcpyKind kind = cudaMemcpyDefault;
+    if (cudaMemcpyAsync(c->U[0].p, u, bu, kind, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync(c->B[0].p, b, bb, kind, c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    c->have_state = true;
+    c->cfl_valid = false;
+    return set_err(mhd_set_time(c, 0.0, INFINITY));
+}
+
+extern "C" MHD_API int mhd_get_state(mhd_ctx* c, void* u, void* b, int where)
+{
+    if (!c || !u || !b || !c->have_state)
+        return set_err(MHD_ERR_ARG);
+    const size_t bu = ncell(c) * 5 * c->elem, bb = ncell(c) * 3 * c->elem;
+    (void)where;  // direction inferred from the pointers (unified addressing)
+    const cudaMemcpyKind kind = cudaMemcpyDefault;
+    if (cudaMemcpyAsync(u, c->U[0].p, bu, kind, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync(b, c->B[0].p, bb, kind, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_state_ptrs(mhd_ctx* c, void** u, void** b)
+{
+    if (!c || !c->have_state)
+        return set_err(MHD_ERR_ARG);
+    if (u)
+        *u = c->U[0].p;
+    if (b)
+        *b = c->B[0].p;
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_set_time(mhd_ctx* c, double t, double tf)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    if (c->elem == 4) {
+        float h[2] = {(float)t, (float)tf};
+        if (cudaMemcpyAsync(c->clock.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+            return set_err(MHD_ERR_CUDA);
+    } else {
+        double h[2] = {t, tf};
+        if (cudaMemcpyAsync(c->clock.p, h, sizeof(h), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+            return set_err(MHD_ERR_CUDA);
+    }
+    if (cudaMemsetAsync(c->nsteps_dev, 0, sizeof(long long), c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_get_time(mhd_ctx* c, double* t, double* dt, long long* steps)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    double clk[4];
+    MHD_TRY(set_err(read_clock(c, clk)));
+    if (t)
+        *t = clk[0];
+    if (dt)
+        *dt = clk[2];
+    if (steps) {
+        if (cudaMemcpy(steps, c->nsteps_dev, sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return set_err(MHD_ERR_CUDA);
+    }
+    return set_err(MHD_OK);
+}
+
+// ------------------------------------------------------------- the step
+
+// One plain Strang step on (U0,B0) -> (U0,B0), C/mhd.c:62-118 with the
+// copy_matrix calls replaced by ping-pong buffers.  Requires cfl_valid (the
+// partials of the current state in c->part): the last fluidx of the step
+// writes the partials of the next state in its epilogue.
+static int enqueue_plain_step(mhd_ctx* c, double cfl)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    void *U0 = c->U[0].p, *U1 = c->U[1].p, *B0 = c->B[0].p, *B1 = c->B[1].p;
+    const void* dt = static_cast<char*>(c->clock.p) + 2 * c->elem;
+    MHD_TRY(op_finalize(c, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
+    // x sweep
+    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt));
+    // y sweep
+    MHD_TRY(op_transpose(c, 1, U0, B0, U1, B1, nx, ny, nz));
+    MHD_TRY(op_fluidx(c, U1, U0, B0, ny, nx, nz, 0, dt, nullptr));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, ny, nx, nz, 0, dt));
+    // z sweep
+    MHD_TRY(op_transpose(c, 2, U0, B0, U1, B1, ny, nx, nz));
+    MHD_TRY(op_fluidx(c, U1, U0, B0, nz, nx, ny, 0, dt, nullptr));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, nz, nx, ny, 0, dt));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nz, nx, ny, 0, dt));
+    MHD_TRY(op_fluidx(c, U0, U1, B0, nz, nx, ny, 0, dt, nullptr));
+    // back
+    MHD_TRY(op_transpose(c, 2, U1, B1, U0, B0, nz, nx, ny));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, ny, nx, nz, 0, dt));
+    MHD_TRY(op_fluidx(c, U0, U1, B0, ny, nx, nz, 0, dt, nullptr));
+    // x again
+    MHD_TRY(op_transpose(c, 1, U1, B1, U0, B0, ny, nx, nz));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt));
+    // last fluidx with the calcfl epilogue for the next step
+    const size_t nparts = (size_t)(ny / fluidx_pencils(nx, ny)) * nz;
+    if (c->part.cap < nparts * c->ks->part_bytes)  // sized by mhd_set_state
+        return MHD_ERR_ARG;
+    MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, c->part.p));
+    c->cfl_nparts = (int)nparts;
+    return MHD_OK;
+}
+
+static int ensure_cfl(mhd_ctx* c)
+{
+    if (c->cfl_valid)
+        return MHD_OK;
+    const size_t cells = ncell(c);
+    MHD_TRY(c->part.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
+    int np = 0;
+    MHD_TRY(op_calcfl_partials(c, c->U[0].p, c->B[0].p, cells, &np));
+    c->cfl_nparts = np;
+    c->cfl_valid = true;
+    return MHD_OK;
+}
+
+static int step_once_direct(mhd_ctx* c, double cfl, int variant)
+{
+    (void)variant;
+    MHD_TRY(ensure_cfl(c));
+    MHD_TRY(enqueue_plain_step(c, cfl));
+    return MHD_OK;
+}
+
+static int step_graph(mhd_ctx* c, double cfl, int variant)
+{
+    MHD_TRY(ensure_cfl(c));
+    // The graph's first node (finalize) reads cfl_nparts partials; those are
+    // written by the previous step's last fluidx, whose grid does not change.
+    const FluidxArgs probe{nullptr, nullptr, nullptr, c->nx, c->ny, c->nz, fluidx_pencils(c->nx, c->ny)};
+    const int steady = (c->ny / probe.P) * c->nz;
+    if (c->cfl_nparts != steady)  // first step after a standalone calcfl
+        return step_once_direct(c, cfl, variant);
+    if (!c->gexec[variant] || c->gcfl[variant] != cfl) {
+        if (c->gexec[variant]) {
+            cudaGraphExecDestroy(c->gexec[variant]);
+            c->gexec[variant] = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        c->capturing = true;
+        const long long before = c->launch_count;
+        int s = enqueue_plain_step(c, cfl);
+        c->capturing = false;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        c->launch_count = before;  // counted per replay below
+        if (s != MHD_OK) {
+            if (g)
+                cudaGraphDestroy(g);
+            return s;
+        }
+        CUDA_TRY(e);
+        size_t nnodes = 0;
+        cudaGraphGetNodes(g, nullptr, &nnodes);
+        c->glaunches[variant] = (int)nnodes;
+        e = cudaGraphInstantiate(&c->gexec[variant], g, 0);
+        cudaGraphDestroy(g);
+        CUDA_TRY(e);
+        c->gcfl[variant] = cfl;
+    }
+    CUDA_TRY(cudaGraphLaunch(c->gexec[variant], c->stream));
+    c->launch_count += c->glaunches[variant];
+    return MHD_OK;
+}
+
+extern "C" MHD_API int mhd_step(mhd_ctx* c, int nsteps, double cfl, int variant)
+{
+    if (!c || !c->have_state || nsteps < 0 || !(cfl > 0) || (variant != MHD_PLAIN && variant != MHD_FUSED))
+        return set_err(MHD_ERR_ARG);
+    if (c->ny != c->nz)  // transpose13 is applied to (ny,nx,nz) and (nz,nx,ny)
+        return set_err(MHD_ERR_UNSUPPORTED);
+    MHD_TRY(set_err(check_dims(c->nx, c->ny, c->nz)));
+    MHD_TRY(set_err(check_dims(c->ny, c->nx, c->nz)));
+    MHD_TRY(set_err(check_dims(c->nz, c->nx, c->ny)));
+    for (int s = 0; s < nsteps; s++) {
+        int st = (c->use_graphs && !c->profile) ? step_graph(c, cfl, variant) : step_once_direct(c, cfl, variant);
+        if (st != MHD_OK)
+            return set_err(st);
+    }
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_use_graphs(mhd_ctx* c, int enable)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    c->use_graphs = enable ? 1 : 0;
+    if (!enable)
+        invalidate_graphs(c);
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_check(mhd_ctx* c)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    int herr = 0;
+    if (cudaMemcpy(&herr, c->err_dev, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    if (herr & DEVERR_TIMEOUT)
+        return set_err(MHD_ERR_TIMEOUT);
+    if (herr & DEVERR_NONFINITE)
+        return set_err(MHD_ERR_NONFINITE);
+    return set_err(MHD_OK);
+}
+
+// -------------------------------------------------------------- profiling
+
+extern "C" MHD_API int mhd_profile(mhd_ctx* c, int enable)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    drain_profile(c);
+    c->profile = enable ? 1 : 0;
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_profile_read(mhd_ctx* c, int kernel, double* total_ms, long long* launches)
+{
+    if (!c || kernel < 0 || kernel >= MHD_K_COUNT)
+        return set_err(MHD_ERR_ARG);
+    drain_profile(c);
+    if (total_ms)
+        *total_ms = c->total_ms[kernel];
+    if (launches)
+        *launches = c->nlaunch[kernel];
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_profile_reset(mhd_ctx* c)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    drain_profile(c);
+    for (int k = 0; k < MHD_K_COUNT; k++) {
+        c->total_ms[k] = 0;
+        c->nlaunch[k] = 0;
+    }
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API long long mhd_launch_count(mhd_ctx* c) { return c ? c->launch_count : -1; }
+
+extern "C" MHD_API int mhd_divb_max(mhd_ctx* c, double* out)
+{
+    if (!c || !out || !c->have_state)
+        return set_err(MHD_ERR_ARG);
+    const size_t cells = ncell(c);
+    const int nparts = (int)((cells + 255) / 256);
+    MHD_TRY(set_err(c->divb.ensure(nparts * sizeof(double))));
+    int np = 0;
+    c->launch_count++;
+    if (c->ks->divb(c->B[0].p, c->nx, c->ny, c->nz, static_cast<double*>(c->divb.p), &np, c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    std::vector<double> h(np);
+    if (cudaMemcpyAsync(h.data(), c->divb.p, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    double m = 0;
+    for (double v : h)
+        m = v > m ? v : m;
+    *out = m;
+    return set_err(MHD_OK);
+}
+
+// ----------------------------------------------------------- drop-in layer
+
+static std::mutex g_dropin_mu;
+static mhd_ctx* g_dropin = nullptr;
+static int g_dropin_mode = -1;
+
+static int dropin_ctx(mhd_ctx** out)
+{
+    if (g_dropin_mode < 0) {
+        const char* m = getenv("MHD_GB300_MODE");
+        g_dropin_mode = (m && (strcmp(m, "exact") == 0 || strcmp(m, "EXACT") == 0)) ? MHD_MODE_EXACT : MHD_MODE_FAST;
+    }
+    if (!g_dropin) {
+        int s = mhd_create(&g_dropin, 1, 1, 1, MHD_F32 | g_dropin_mode);
+        if (s != MHD_OK)
+            return s;
+    }
+    *out = g_dropin;
+    return MHD_OK;
+}
+
+extern "C" MHD_API int mhd_set_dropin_mode(int mode)
+{
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (mode != MHD_MODE_FAST && mode != MHD_MODE_EXACT)
+        return set_err(MHD_ERR_ARG);
+    g_dropin_mode = mode;
+    if (g_dropin) {
+        g_dropin->flags = MHD_F32 | mode;
+        g_dropin->ks = pick_set(g_dropin->flags);
+    }
+    return set_err(MHD_OK);
+}
+
+// A drop-in argument: device-accessible pointers are used in place; host
+// memory is staged through a cached device mirror (copied in if read, copied
+// back if written).
+struct Arg {
+    void* user;
+    size_t bytes;
+    bool in, out;
+    void* dev = nullptr;
+    bool staged = false;
+};
+
+static bool device_accessible(const void* p)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+static int stage_in(mhd_ctx* c, Arg* args, int na)
+{
+    int slot = 0;
+    for (int s = 0; s < na; s++) {
+        Arg& a = args[s];
+        // the same user pointer twice shares one mirror
+        for (int t = 0; t < s; t++)
+            if (args[t].user == a.user && args[t].bytes == a.bytes) {
+                a.dev = args[t].dev;
+                a.staged = args[t].staged;
+                break;
+            }
+        if (a.dev)
+            continue;
+        if (device_accessible(a.user)) {
+            a.dev = a.user;
+            continue;
+        }
+        MHD_TRY(c->stage[slot].ensure(a.bytes));
+        a.dev = c->stage[slot].p;
+        a.staged = true;
+        slot++;
+        if (a.in)
+            CUDA_TRY(cudaMemcpyAsync(a.dev, a.user, a.bytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    return MHD_OK;
+}
+
+static int stage_out(mhd_ctx* c, Arg* args, int na)
+{
+    for (int s = 0; s < na; s++) {
+        Arg& a = args[s];
+        bool first = true;
+        for (int t = 0; t < s; t++)
+            if (args[t].user == a.user && args[t].out)
+                first = false;
+        if (a.staged && a.out && first)
+            CUDA_TRY(cudaMemcpyAsync(a.user, a.dev, a.bytes, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MHD_OK;
+}
+
+static bool dims_ok(const int* nx, const int* ny, const int* nz)
+{
+    return nx && ny && nz && *nx >= 0 && *ny >= 0 && *nz >= 0;
+}
+
+static size_t cells_of(const int* nx, const int* ny, const int* nz) { return (size_t)(*nx) * (*ny) * (*nz); }
+
+extern "C" MHD_API void fluidx(float* u, float* b, int* nx, int* ny, int* nz, float* dt, float* update_u,
+                               float* update_b, int iter)
+{
+    (void)b;
+    (void)iter;
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !update_u || !update_b || !dt || !dims_ok(nx, ny, nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    const size_t cells = cells_of(nx, ny, nz);
+    if (cells == 0) {
+        set_err(MHD_OK);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    Arg args[3] = {{update_u, cells * 20, true, false}, {update_b, cells * 12, true, false}, {u, cells * 20, false, true}};
+    if (set_err(stage_in(c, args, 3)) != MHD_OK)
+        return;
+    if (set_err(op_fluidx(c, args[2].dev, args[0].dev, args[1].dev, *nx, *ny, *nz, (double)*dt, nullptr, nullptr)) !=
+        MHD_OK)
+        return;
+    set_err(stage_out(c, args, 3));
+}
+
+extern "C" MHD_API void advectbyzx(float* u, float* b, int* nx, int* ny, int* nz, float* dt, float* update_u,
+                                   float* update_b)
+{
+    (void)u;
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!b || !update_u || !update_b || !dt || !dims_ok(nx, ny, nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    const size_t cells = cells_of(nx, ny, nz);
+    if (cells == 0) {
+        set_err(MHD_OK);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    Arg args[3] = {{update_u, cells * 20, true, false}, {update_b, cells * 12, true, false}, {b, cells * 12, true, true}};
+    if (set_err(stage_in(c, args, 3)) != MHD_OK)
+        return;
+    const void* ub = args[1].dev;
+    if (args[2].dev == ub) {  // b and update_b alias: keep a private copy of the input
+        if (set_err(c->alias[1].ensure(cells * 12)) != MHD_OK || set_err(op_copy(c, ub, c->alias[1].p, cells * 12)) != MHD_OK)
+            return;
+        ub = c->alias[1].p;
+    }
+    if (set_err(op_advect(c, args[2].dev, args[2].dev, args[0].dev, ub, *nx, *ny, *nz, (double)*dt, nullptr)) !=
+        MHD_OK)
+        return;
+    set_err(stage_out(c, args, 3));
+}
+
+static void dropin_transpose(int axis, float* u, float* b, float* update_u, float* update_b, int* nx, int* ny, int* nz)
+{
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !b || !update_u || !update_b || !dims_ok(nx, ny, nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    if (axis == 2 && *nx != *nz) {  // C/transpose13.c:50-61 leaves the outputs untouched
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    const size_t cells = cells_of(nx, ny, nz);
+    if (cells == 0) {
+        set_err(MHD_OK);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    Arg args[4] = {{update_u, cells * 20, true, false},
+                   {update_b, cells * 12, true, false},
+                   {u, cells * 20, false, true},
+                   {b, cells * 12, false, true}};
+    if (set_err(stage_in(c, args, 4)) != MHD_OK)
+        return;
+    if (set_err(transpose_entry(c, axis, args[2].dev, args[3].dev, args[0].dev, args[1].dev, *nx, *ny, *nz)) != MHD_OK)
+        return;
+    set_err(stage_out(c, args, 4));
+}
+
+extern "C" MHD_API void transpose12(float* u, float* b, float* update_u, float* update_b, int* nx, int* ny, int* nz,
+                                    int iter)
+{
+    (void)iter;
+    dropin_transpose(1, u, b, update_u, update_b, nx, ny, nz);
+}
+
+extern "C" MHD_API void transpose13(float* u, float* b, float* update_u, float* update_b, int* nx, int* ny, int* nz)
+{
+    dropin_transpose(2, u, b, update_u, update_b, nx, ny, nz);
+}
+
+extern "C" MHD_API void copy_matrix(float* u, float* b, int* nx, int* ny, int* nz, float* update_u, float* update_b)
+{
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !b || !update_u || !update_b || !dims_ok(nx, ny, nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    const size_t cells = cells_of(nx, ny, nz);
+    if (cells == 0) {
+        set_err(MHD_OK);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    Arg args[4] = {{u, cells * 20, true, false},
+                   {b, cells * 12, true, false},
+                   {update_u, cells * 20, false, true},
+                   {update_b, cells * 12, false, true}};
+    if (set_err(stage_in(c, args, 4)) != MHD_OK)
+        return;
+    if (set_err(op_copy(c, args[0].dev, args[2].dev, cells * 20)) != MHD_OK ||
+        set_err(op_copy(c, args[1].dev, args[3].dev, cells * 12)) != MHD_OK)
+        return;
+    set_err(stage_out(c, args, 4));
+}
+
+extern "C" MHD_API float calcfl(float* u, float* b, int* nx, int* ny, int* nz)
+{
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !b || !dims_ok(nx, ny, nz)) {
+        set_err(MHD_ERR_ARG);
+        return NAN;
+    }
+    const size_t cells = cells_of(nx, ny, nz);
+    if (cells == 0) {
+        set_err(MHD_OK);
+        return INFINITY;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return NAN;
+    Arg args[2] = {{u, cells * 20, true, false}, {b, cells * 12, true, false}};
+    if (set_err(stage_in(c, args, 2)) != MHD_OK)
+        return NAN;
+    double inv = NAN;
+    int s = calcfl_sync(c, args[0].dev, args[1].dev, *nx, *ny, *nz, &inv);
+    set_err(s);
+    return (float)inv;
+}

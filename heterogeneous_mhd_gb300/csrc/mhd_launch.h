@@ -1,0 +1,35 @@
+// Host-side view of the kernel sets.  Each set is one (precision, arithmetic
+// policy) instantiation of the kernels in mhd_kernels.cuh; the FAST set is
+// compiled with FMA contraction, the EXACT sets with --fmad=false.
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "mhd_kernels.cuh"
+
+namespace mhd {
+
+struct KernelSet {
+    int elem;  // sizeof(R)
+    int exact; // reproduces the reference bit for bit
+    cudaError_t (*fluidx)(const FluidxArgs&, cudaStream_t);
+    cudaError_t (*advect)(const AdvectArgs&, cudaStream_t);
+    cudaError_t (*transpose)(const TransposeArgs&, cudaStream_t);
+    // first CFL pass over ncell cells; returns the number of partials written
+    cudaError_t (*calcfl)(const void* u, const void* b, size_t ncell, void* part, int* nparts, cudaStream_t);
+    cudaError_t (*cfl_finalize)(const CflFinalizeArgs&, cudaStream_t);
+    cudaError_t (*divb)(const void* b, int nx, int ny, int nz, double* part, int* nparts, cudaStream_t);
+    size_t part_bytes; // sizeof(CflPart<R>)
+};
+
+const KernelSet* kernels_f32_fast();
+const KernelSet* kernels_f32_exact();
+const KernelSet* kernels_f64_exact();
+
+// Pencils per CTA along j for fluidx / advectbyzx (a divisor of ny).
+int fluidx_pencils(int nx, int ny);
+int advect_pencils(int nx, int ny);
+
+cudaError_t launch_copy(const void* src, void* dst, size_t bytes, cudaStream_t s);
+
+}  // namespace mhd

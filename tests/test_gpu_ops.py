@@ -1,0 +1,178 @@
+"""Per-operator parity of the sm_103a kernels against the C oracle.
+
+EXACT kernels: bit-for-bit against the golden fixtures of the reference's own
+C/ sources and against the oracle restatement on further shapes.  FAST
+kernels (FMA contraction, reciprocal multiplies): relative L2 per operator
+below 1e-6 in FP32.
+"""
+import numpy as np
+import pytest
+
+from util import bitwise_equal, load_npz, rel_l2, shapes_in
+
+pytestmark = pytest.mark.gpu
+DT = 0.05
+FAST_OP_TOL = 1e-6  # relative L2 of one operator application, FP32
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def run_ops(mhd, torch, ctx, u, b, bin_, nx, ny, nz):
+    du, db = dev(torch, u), dev(torch, b)
+    out = {}
+    uo = torch.full_like(du, 7)
+    ctx.op_fluidx(uo, du, db, nx, ny, nz, DT)
+    bo = dev(torch, bin_)
+    ctx.op_advectbyzx(bo, du, db, nx, ny, nz, DT)
+    ut, bt = torch.empty_like(du), torch.empty_like(db)
+    ctx.op_transpose12(ut, bt, du, db, nx, ny, nz)
+    ctx.sync()
+    out["fluidx_u"], out["advect_b"], out["t12_u"], out["t12_b"] = host(uo), host(bo), host(ut), host(bt)
+    if nx == nz:
+        ut, bt = torch.empty_like(du), torch.empty_like(db)
+        ctx.op_transpose13(ut, bt, du, db, nx, ny, nz)
+        ctx.sync()
+        out["t13_u"], out["t13_b"] = host(ut), host(bt)
+    out["calcfl"] = np.array([ctx.op_calcfl(du, db, nx, ny, nz)], dtype=u.dtype)
+    return out
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_exact_ops_bitwise_vs_reference_golden(bits, mhd, cuda):
+    fix = load_npz(f"ops_f{bits}.npz")
+    with mhd.Context(1, 1, 1, fp64=(bits == 64), exact=True) as ctx:
+        for nx, ny, nz in shapes_in(fix):
+            key = f"{nx}x{ny}x{nz}"
+            out = run_ops(mhd, cuda, ctx, fix[f"{key}/u"], fix[f"{key}/b"], fix[f"{key}/advect_bin"], nx, ny, nz)
+            for name, got in out.items():
+                assert bitwise_equal(got, fix[f"{key}/{name}"]), f"{name} {key} f{bits}"
+
+
+def test_fast_ops_close_to_reference_golden(mhd, cuda):
+    fix = load_npz("ops_f32.npz")
+    with mhd.Context(1, 1, 1) as ctx:
+        for nx, ny, nz in shapes_in(fix):
+            key = f"{nx}x{ny}x{nz}"
+            out = run_ops(mhd, cuda, ctx, fix[f"{key}/u"], fix[f"{key}/b"], fix[f"{key}/advect_bin"], nx, ny, nz)
+            for name, got in out.items():
+                ref = fix[f"{key}/{name}"]
+                if name.startswith("t1"):
+                    assert bitwise_equal(got, ref), name  # data movement is exact in every mode
+                else:
+                    assert rel_l2(got, ref) < FAST_OP_TOL, f"{name} {key}: {rel_l2(got, ref):.2e}"
+
+
+SHAPES = [(64, 64, 64), (48, 48, 48), (256, 8, 4), (100, 6, 5), (512, 2, 2), (96, 12, 96), (3, 5, 7), (4, 1, 1)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_exact_ops_bitwise_vs_oracle(shape, mhd, cuda, oracle32):
+    """More shapes: TMA and plain staging, warp and generic pencil reductions,
+    multi-pencil CTAs, the largest supported pencil (512)."""
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx * 7 + ny)
+    u, b = mhd.init_vortex(nx, ny, nz, seed=int(rng.integers(1 << 20)))
+    u = (u * (1 + 0.05 * rng.standard_normal(u.shape))).astype(np.float32)
+    b = (b + 0.05 * rng.standard_normal(b.shape)).astype(np.float32)
+    bin_ = (b * np.float32(0.75)).astype(np.float32)
+    ref = {}
+    uo = np.full_like(u, 7)
+    oracle32.fluidx(uo, b.copy(), nx, ny, nz, DT, u.copy(), b.copy())
+    ref["fluidx_u"] = uo
+    bo = bin_.copy()
+    oracle32.advectbyzx(u.copy(), bo, nx, ny, nz, DT, u.copy(), b.copy())
+    ref["advect_b"] = bo
+    ut, bt = np.empty_like(u), np.empty_like(b)
+    oracle32.transpose12(ut, bt, u.copy(), b.copy(), nx, ny, nz)
+    ref["t12_u"], ref["t12_b"] = ut, bt
+    if nx == nz:
+        ut, bt = np.empty_like(u), np.empty_like(b)
+        oracle32.transpose13(ut, bt, u.copy(), b.copy(), nx, ny, nz)
+        ref["t13_u"], ref["t13_b"] = ut, bt
+    ref["calcfl"] = np.array([oracle32.calcfl(u, b, nx, ny, nz)], dtype=np.float32)
+    with mhd.Context(1, 1, 1, exact=True) as ctx:
+        out = run_ops(mhd, cuda, ctx, u, b, bin_, nx, ny, nz)
+    for name in ref:
+        assert bitwise_equal(out[name], ref[name]), f"{name} {shape}"
+    with mhd.Context(1, 1, 1) as ctx:
+        out = run_ops(mhd, cuda, ctx, u, b, bin_, nx, ny, nz)
+    for name in ("fluidx_u", "advect_b", "calcfl"):
+        assert rel_l2(out[name], ref[name]) < FAST_OP_TOL, f"{name} {shape}"
+
+
+def test_in_place_and_aliased_arguments(mhd, cuda, oracle32):
+    """The reference's C/ allows u == update_u for fluidx and b == update_b for
+    advectbyzx and the transposes (it works pencil by pencil / plane by plane);
+    the GPU entry points keep those semantics."""
+    torch = cuda
+    nx = ny = nz = 16
+    u, b = mhd.init_vortex(nx, ny, nz, seed=2)
+    with mhd.Context(1, 1, 1, exact=True) as ctx:
+        uo = np.full_like(u, 7)
+        oracle32.fluidx(uo, b.copy(), nx, ny, nz, DT, u.copy(), b.copy())
+        du, db = dev(torch, u), dev(torch, b)
+        ctx.op_fluidx(du, du, db, nx, ny, nz, DT)
+        ctx.sync()
+        assert bitwise_equal(host(du), uo)
+        bref = b.copy()
+        oracle32.advectbyzx(u.copy(), bref, nx, ny, nz, DT, u.copy(), bref)
+        du, db = dev(torch, u), dev(torch, b)
+        ctx.op_advectbyzx(db, du, db, nx, ny, nz, DT)
+        ctx.sync()
+        assert bitwise_equal(host(db), bref)
+        ut, bt = u.copy(), b.copy()
+        oracle32.transpose12(ut, bt, ut, bt, nx, ny, nz)
+        du, db = dev(torch, u), dev(torch, b)
+        ctx.op_transpose12(du, db, du, db, nx, ny, nz)
+        ctx.sync()
+        assert bitwise_equal(host(du), ut) and bitwise_equal(host(db), bt)
+
+
+def test_transpose13_rejects_non_square(mhd, cuda):
+    torch = cuda
+    u = torch.arange(5 * 4 * 3 * 2, dtype=torch.float32, device="cuda")
+    b = torch.arange(3 * 4 * 3 * 2, dtype=torch.float32, device="cuda")
+    uo, bo = torch.full_like(u, -1), torch.full_like(b, -1)
+    with mhd.Context(1, 1, 1) as ctx:
+        with pytest.raises(mhd.MhdError) as e:
+            ctx.op_transpose13(uo, bo, u, b, 4, 3, 2)
+        assert e.value.status == 1
+    assert bool((uo == -1).all()) and bool((bo == -1).all())
+
+
+@pytest.mark.parametrize("where", ["middle", "last", "none"])
+def test_calcfl_nan_semantics(where, mhd, cuda, oracle32):
+    """max_2num (C/calcfl.c:91-101) restarts the running max after a NaN cell;
+    a NaN in the last cell makes the result NaN."""
+    nx, ny, nz = 24, 8, 8
+    u, b = mhd.init_vortex(nx, ny, nz, seed=5)
+    nc = nx * ny * nz
+    if where != "none":
+        cell = nc // 2 if where == "middle" else nc - 1
+        u[cell * 5] = np.nan
+    ref = oracle32.calcfl(u, b, nx, ny, nz)
+    for exact in (True, False):
+        with mhd.Context(1, 1, 1, exact=exact) as ctx:
+            got = ctx.op_calcfl(dev(cuda, u), dev(cuda, b), nx, ny, nz)
+        if where == "last":
+            assert np.isnan(got) and np.isnan(ref)
+        elif exact:
+            assert np.float32(got) == np.float32(ref)
+        else:
+            assert abs(got - ref) <= 2e-6 * abs(ref)
+
+
+def test_empty_grid(mhd, cuda):
+    """Zero cells: the reference's calcfl returns 1/0 = inf; the operators do nothing."""
+    u = np.zeros(5, dtype=np.float32)
+    b = np.zeros(3, dtype=np.float32)
+    assert mhd.calcfl(u, b, 0, 4, 4) == float("inf")
+    uo = np.full(5, 3, dtype=np.float32)
+    mhd.fluidx(uo, b, 0, 4, 4, 0.1, u, b)
+    assert (uo == 3).all()

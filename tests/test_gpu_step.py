@@ -1,0 +1,185 @@
+"""Whole Strang steps (C/mhd.c:59-124) on the GPU against the C oracle.
+
+* EXACT: bit-for-bit with the reference (golden fixtures, 64^3 checksums
+  after 1, 10 and 100 steps, FP32 and FP64).
+* FAST (the production path): relative L2 per field <= 1e-5 after one step
+  (the stated FP32 tolerance) and <= FAST_100_TOL after 100 steps of the
+  64^3 vortex; div B at FP32 round-off; conservation.
+* Full size: one 256^3 turbulence step against the oracle, and 512^3
+  properties (div B, conservation, agreement with the EXACT kernels).
+"""
+import json
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from util import bitwise_equal, checksums, load_npz, rel_l2_fields, sha, shapes_in
+
+pytestmark = pytest.mark.gpu
+
+STEP1_TOL = 1e-5      # relative L2 per field after one Strang step (FP32)
+FAST_100_TOL = 5e-3   # relative L2 per field after 100 steps of the 64^3 vortex
+DIVB_TOL = 2e-6       # max |div B| / max |B| in FP32
+
+
+def run(mhd, u0, b0, shape, nsteps, exact=False, fp64=False, cfl=0.7, graphs=True):
+    with mhd.Context(*shape, fp64=fp64, exact=exact) as ctx:
+        ctx.use_graphs(graphs)
+        ctx.set_state(u0, b0)
+        ctx.step(nsteps, cfl=cfl)
+        u, b = ctx.get_state()
+        t, dt, s = ctx.time()
+        assert ctx.check() == mhd.MHD_OK
+        assert s == nsteps
+    return u, b, t
+
+
+def record(name, value):
+    out = Path(os.environ.get("GRAFT_REPO_ROOT", ".")) / "gpurun_out"
+    if out.is_dir():
+        p = out / "parity_metrics.json"
+        d = json.loads(p.read_text()) if p.exists() else {}
+        d[name] = value
+        p.write_text(json.dumps(d, indent=1))
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_exact_steps_bitwise_vs_reference_golden(bits, mhd, cuda):
+    fix = load_npz(f"steps_f{bits}.npz")
+    for nx, ny, nz in shapes_in(fix):
+        key = f"{nx}x{ny}x{nz}"
+        u0, b0 = mhd.init_vortex(nx, ny, nz, seed=7, fp64=(bits == 64))
+        assert sha(u0, b0) == str(fix[f"{key}/init_sha256"][0])
+        n = int(fix[f"{key}/nsteps"][0])
+        for graphs in (True, False):
+            u, b, t = run(mhd, u0, b0, (nx, ny, nz), n, exact=True, fp64=(bits == 64), graphs=graphs)
+            assert bitwise_equal(u, fix[f"{key}/u"]) and bitwise_equal(b, fix[f"{key}/b"]), (key, graphs)
+            assert np.array(t, dtype=u.dtype) == fix[f"{key}/t"][0]
+
+
+def test_exact_64_vortex_checksums_fp32(mhd, cuda):
+    """Config 1 (64^3, CFL 0.7): the reference's state hash after 1, 10, 100 steps."""
+    ck = checksums()["f32"]
+    u0, b0 = mhd.init_vortex(64, 64, 64, seed=0)
+    assert sha(u0, b0) == ck["init"]
+    with mhd.Context(64, 64, 64, exact=True) as ctx:
+        ctx.set_state(u0, b0)
+        done = 0
+        for target in (1, 10, 100):
+            ctx.step(target - done, cfl=0.7)
+            done = target
+            u, b = ctx.get_state()
+            assert sha(u, b) == ck[str(target)]["sha256"], f"after {target} steps"
+            t, _, _ = ctx.time()
+            assert np.float32(t) == np.float32(ck[str(target)]["t"])
+
+
+def test_exact_64_vortex_checksums_fp64(mhd, cuda):
+    ck = checksums()["f64"]
+    u0, b0 = mhd.init_vortex(64, 64, 64, seed=0, fp64=True)
+    assert sha(u0, b0) == ck["init"]
+    with mhd.Context(64, 64, 64, fp64=True) as ctx:
+        ctx.set_state(u0, b0)
+        ctx.step(1, cfl=0.7)
+        u, b = ctx.get_state()
+        assert sha(u, b) == ck["1"]["sha256"]
+        ctx.step(9, cfl=0.7)
+        u, b = ctx.get_state()
+        assert sha(u, b) == ck["10"]["sha256"]
+
+
+def test_fast_64_vortex_tolerance(mhd, cuda, oracle32, oracle64):
+    """Config 1 with the production kernels: per-field relative L2 against the
+    reference C after 1 and 100 steps, and the FP32-vs-FP64 error of both."""
+    u0, b0 = mhd.init_vortex(64, 64, 64, seed=0)
+    s = (64, 64, 64)
+    ref1 = oracle32.strang(u0, b0, *s, 1)
+    ref100 = oracle32.strang(ref1[0], ref1[1], *s, 99, t=ref1[2])
+    u1, b1, _ = run(mhd, u0, b0, s, 1)
+    e1 = rel_l2_fields(u1, b1, ref1[0], ref1[1])
+    u100, b100, _ = run(mhd, u0, b0, s, 100)
+    e100 = rel_l2_fields(u100, b100, ref100[0], ref100[1])
+    u64, b64 = mhd.init_vortex(64, 64, 64, seed=0, fp64=True)
+    r64 = oracle64.strang(u64, b64, *s, 100)
+    e_fast_vs_f64 = rel_l2_fields(u100, b100, r64[0], r64[1])
+    e_ref_vs_f64 = rel_l2_fields(ref100[0], ref100[1], r64[0], r64[1])
+    record("vortex64_fast_vs_ref_step1", e1)
+    record("vortex64_fast_vs_ref_step100", e100)
+    record("vortex64_fast_vs_fp64_step100", e_fast_vs_f64)
+    record("vortex64_ref_vs_fp64_step100", e_ref_vs_f64)
+    assert max(e1.values()) <= STEP1_TOL, e1
+    assert max(e100.values()) <= FAST_100_TOL, e100
+
+
+def test_fast_divb_and_conservation(mhd, cuda):
+    n = 64
+    u0, b0 = mhd.init_turbulence(n, seed=1)
+    u, b, _ = run(mhd, u0, b0, (n, n, n), 10)
+    bmax = float(np.abs(b).max())
+    divb = mhd.host_divb_max(b, n, n, n)
+    record("turb64_divb_rel_step10", divb / bmax)
+    assert divb / bmax < DIVB_TOL
+    U0, U = u0.reshape(-1, 5).astype(np.float64), u.reshape(-1, 5).astype(np.float64)
+    for c in range(5):  # flux-form update: totals change only by round-off
+        assert abs(U[:, c].sum() - U0[:, c].sum()) <= 1e-5 * np.abs(U0[:, c]).sum() + 1e-6, c
+    B0, B = b0.reshape(-1, 3).astype(np.float64), b.reshape(-1, 3).astype(np.float64)
+    for c in range(3):
+        assert abs(B[:, c].sum() - B0[:, c].sum()) <= 1e-5 * np.abs(B0[:, c]).sum() + 1e-6, c
+
+
+def test_graph_replay_matches_direct_launches(mhd, cuda):
+    n = 32
+    u0, b0 = mhd.init_turbulence(n, seed=2)
+    a = run(mhd, u0, b0, (n, n, n), 4, graphs=True)
+    b = run(mhd, u0, b0, (n, n, n), 4, graphs=False)
+    assert bitwise_equal(a[0], b[0]) and bitwise_equal(a[1], b[1])
+
+
+def test_tf_clamp_and_time(mhd, cuda, oracle32):
+    """dt clamp to (tf-t)/2 and t += 2dt (C/mhd.c:63-64), on the device clock."""
+    n = 16
+    u0, b0 = mhd.init_vortex(n, n, n, seed=3)
+    ref = oracle32.strang(u0, b0, n, n, n, 5, cfl=0.9, tf=1.5)
+    with mhd.Context(n, n, n, exact=True) as ctx:
+        ctx.set_state(u0, b0)
+        ctx.set_time(0.0, 1.5)
+        ctx.step(ref[4], cfl=0.9)
+        u, b = ctx.get_state()
+        t, _, _ = ctx.time()
+    assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1])
+    assert np.float32(t) == np.float32(ref[2]) == np.float32(1.5)
+
+
+def test_full_size_256_turbulence_vs_oracle(mhd, cuda, oracle32):
+    """Config 2 at full size (256^3): one step of the production kernels
+    against the reference C (oracle), and the EXACT kernels bit for bit."""
+    n = 256
+    u0, b0 = mhd.init_turbulence(n, seed=0)
+    ref = oracle32.strang(u0, b0, n, n, n, 1)
+    uf, bf, _ = run(mhd, u0, b0, (n, n, n), 1)
+    e = rel_l2_fields(uf, bf, ref[0], ref[1])
+    record("turb256_fast_vs_ref_step1", e)
+    assert max(e.values()) <= STEP1_TOL, e
+    ue, be, _ = run(mhd, u0, b0, (n, n, n), 1, exact=True)
+    assert bitwise_equal(ue, ref[0]) and bitwise_equal(be, ref[1])
+
+
+def test_full_size_512_properties(mhd, cuda):
+    """512^3 (the largest configuration): FAST vs EXACT after one step, div B,
+    and mass conservation, without a CPU run."""
+    n = 512
+    u0, b0 = mhd.init_turbulence(n, seed=1)
+    uf, bf, _ = run(mhd, u0, b0, (n, n, n), 1)
+    ue, be, _ = run(mhd, u0, b0, (n, n, n), 1, exact=True)
+    e = rel_l2_fields(uf, bf, ue, be)
+    record("turb512_fast_vs_exact_step1", e)
+    assert max(e.values()) <= STEP1_TOL, e
+    assert np.isfinite(uf).all() and np.isfinite(bf).all()
+    divb = mhd.host_divb_max(bf, n, n, n) / float(np.abs(bf).max())
+    record("turb512_divb_rel_step1", divb)
+    assert divb < DIVB_TOL
+    m0 = u0.reshape(-1, 5)[:, 0].astype(np.float64).sum()
+    m1 = uf.reshape(-1, 5)[:, 0].astype(np.float64).sum()
+    assert abs(m1 - m0) <= 1e-5 * m0
