@@ -1,57 +1,223 @@
 // Launcher bodies shared by the kernel-set translation units.  Included once
 // per unit with MHD_SET_NAME, MHD_REAL and MHD_EXACT defined.
+//
+// Each operator has a register-resident kernel for the common pencil lengths
+// (fluidx: n = 4T with T in {8..128} or 3T with T in {16..128}; advectbyzx:
+// n = 8T, T in {4..64} or 6T, T in {8..64}; transposes: full 32x32 tiles) and
+// a general kernel for every other shape.  FP64 uses the general kernels.
+#include "mhd_advect2.cuh"
+#include "mhd_fluidx2.cuh"
 #include "mhd_launch.h"
+#include "mhd_transpose2.cuh"
 
 namespace mhd {
 namespace MHD_SET_NAME {
 
 using R = MHD_REAL;
 constexpr bool EX = MHD_EXACT;
+constexpr bool kV2 = (sizeof(R) == 4);
 
-static cudaError_t fluidx(const FluidxArgs& a, cudaStream_t s)
+// Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum
+// minus its static shared memory (once per kernel).
+template <typename K>
+static cudaError_t allow_smem(K kernel, bool& done)
+{
+    if (done)
+        return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&fa, kernel);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess)
+        done = true;
+    return e;
+}
+
+static bool pow2_in(int T, int lo, int hi) { return T >= lo && T <= hi && (T & (T - 1)) == 0; }
+
+// ------------------------------------------------------------------ fluidx
+
+struct FxPlan {
+    int C, T, P;  // C == 0: general kernel with P pencils per CTA
+};
+
+static FxPlan plan_fluidx(int nx, int ny, bool aligned)
+{
+    FxPlan p{0, 0, 0};
+    if (kV2 && aligned) {
+        if (nx % 4 == 0 && pow2_in(nx / 4, 8, 128))
+            p.C = 4, p.T = nx / 4;
+        else if (nx % 3 == 0 && nx % 4 == 0 && pow2_in(nx / 3, 16, 128))
+            p.C = 3, p.T = nx / 3;
+        if (p.C) {
+            p.P = 0;
+            for (int P = 1; P <= ny; P++)
+                if (ny % P == 0 && P * p.T <= 128 && (P * p.T) % 32 == 0)
+                    p.P = P;
+            if (p.P)
+                return p;
+        }
+    }
+    p.C = p.T = 0;
+    p.P = fluidx_pencils(nx, ny);
+    return p;
+}
+
+template <int C, int T>
+static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    const size_t smem = fluidx_smem_elems(a.nx, a.P) * sizeof(R);
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_fluidx<R, EX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e != cudaSuccess)
-            return e;
-        attr = true;
-    }
+    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T>, attr);
+    if (e != cudaSuccess)
+        return e;
     dim3 grid(a.ny / a.P, a.nz);
-    k_fluidx<R, EX><<<grid, fluidx_threads(a.nx, a.P), smem, s>>>(a);
+    k_fluidx2<R, EX, C, T><<<grid, a.P * T, fluidx2_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
     return cudaGetLastError();
 }
 
-static cudaError_t advect(const AdvectArgs& a, cudaStream_t s)
+static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
+{
+    FluidxArgs a = in;
+    const FxPlan p = plan_fluidx(a.nx, a.ny, a.use_tma != 0);
+    a.P = p.P;
+    if constexpr (kV2) {
+        if (p.C == 4) {
+            switch (p.T) {
+            case 8: return launch_fx2<4, 8>(a, s);
+            case 16: return launch_fx2<4, 16>(a, s);
+            case 32: return launch_fx2<4, 32>(a, s);
+            case 64: return launch_fx2<4, 64>(a, s);
+            case 128: return launch_fx2<4, 128>(a, s);
+            }
+        } else if (p.C == 3) {
+            switch (p.T) {
+            case 16: return launch_fx2<3, 16>(a, s);
+            case 32: return launch_fx2<3, 32>(a, s);
+            case 64: return launch_fx2<3, 64>(a, s);
+            case 128: return launch_fx2<3, 128>(a, s);
+            }
+        }
+    }
+    static bool attr = false;
+    cudaError_t e = allow_smem(k_fluidx<R, EX>, attr);
+    if (e != cudaSuccess)
+        return e;
+    dim3 grid(a.ny / a.P, a.nz);
+    k_fluidx<R, EX><<<grid, fluidx_threads(a.nx, a.P), fluidx_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
+    return cudaGetLastError();
+}
+
+static int fluidx_parts(int nx, int ny, int nz, int aligned)
+{
+    const FxPlan p = plan_fluidx(nx, ny, aligned != 0);
+    return (ny / p.P) * nz;
+}
+
+// -------------------------------------------------------------- advectbyzx
+
+static FxPlan plan_advect(int nx, int ny, bool aligned)
+{
+    FxPlan p{0, 0, 0};
+    if (kV2 && aligned) {
+        if (nx % 8 == 0 && pow2_in(nx / 8, 4, 64))
+            p.C = 8, p.T = nx / 8;
+        else if (nx % 6 == 0 && pow2_in(nx / 6, 8, 64))
+            p.C = 6, p.T = nx / 6;
+        if (p.C) {
+            p.P = 0;
+            for (int P = 1; P <= ny && P <= 32; P++)
+                if (ny % P == 0 && advect2_threads(P, p.T) <= 512)
+                    p.P = P;
+            if (p.P)
+                return p;
+        }
+    }
+    p.C = p.T = 0;
+    p.P = advect_pencils(nx, ny);
+    return p;
+}
+
+template <int C, int T>
+static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    const size_t smem = advect_smem_elems(a.nx, a.P) * sizeof(R);
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_advect<R, EX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e != cudaSuccess)
-            return e;
-        attr = true;
+    cudaError_t e = allow_smem(k_advect2<R, EX, C, T>, attr);
+    if (e != cudaSuccess)
+        return e;
+    dim3 grid(a.ny / a.P, a.nz);
+    k_advect2<R, EX, C, T><<<grid, advect2_threads(a.P, T), advect2_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
+    return cudaGetLastError();
+}
+
+static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
+{
+    AdvectArgs a = in;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
+                         reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
+    const FxPlan p = plan_advect(a.nx, a.ny, (al & 15) == 0);
+    a.P = p.P;
+    if constexpr (kV2) {
+        if (p.C == 8) {
+            switch (p.T) {
+            case 4: return launch_ad2<8, 4>(a, s);
+            case 8: return launch_ad2<8, 8>(a, s);
+            case 16: return launch_ad2<8, 16>(a, s);
+            case 32: return launch_ad2<8, 32>(a, s);
+            case 64: return launch_ad2<8, 64>(a, s);
+            }
+        } else if (p.C == 6) {
+            switch (p.T) {
+            case 8: return launch_ad2<6, 8>(a, s);
+            case 16: return launch_ad2<6, 16>(a, s);
+            case 32: return launch_ad2<6, 32>(a, s);
+            case 64: return launch_ad2<6, 64>(a, s);
+            }
+        }
     }
+    static bool attr = false;
+    cudaError_t e = allow_smem(k_advect<R, EX>, attr);
+    if (e != cudaSuccess)
+        return e;
     int threads = ((a.nx * a.P + 31) / 32) * 32;
     if (threads > 512)
         threads = 512;
     if (threads < 128)
         threads = 128;
     dim3 grid(a.ny / a.P, a.nz);
-    k_advect<R, EX><<<grid, threads, smem, s>>>(a);
+    k_advect<R, EX><<<grid, threads, advect_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
     return cudaGetLastError();
 }
 
+// -------------------------------------------------------------- transposes
+
 static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
 {
-    constexpr int T = TTile<R>::E;
     const int na = (a.axis == 1) ? a.ny : a.nz;
     const int nb = (a.axis == 1) ? a.nz : a.ny;
+    if constexpr (kV2) {
+        const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.b_out) |
+                             reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
+        if (a.nx % kT2 == 0 && na % kT2 == 0 && (al & 3) == 0) {
+            dim3 grid(a.nx / kT2, na / kT2, nb);
+            if (a.axis == 1)
+                k_transpose2<1><<<grid, 256, 0, s>>>(a);
+            else
+                k_transpose2<2><<<grid, 256, 0, s>>>(a);
+            return cudaGetLastError();
+        }
+    }
+    constexpr int T = TTile<R>::E;
     dim3 grid((a.nx + T - 1) / T, (na + T - 1) / T, nb);
     k_transpose<R><<<grid, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
+
+// ------------------------------------------------------------------ calcfl
 
 static cudaError_t calcfl(const void* u, const void* b, size_t ncell, void* part, int* nparts, cudaStream_t s)
 {
@@ -78,7 +244,7 @@ static cudaError_t divb(const void* b, int nx, int ny, int nz, double* part, int
 }
 
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
-                               sizeof(CflPart<R>)};
+                               sizeof(CflPart<R>), fluidx_parts};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

@@ -129,6 +129,19 @@ struct mhd_ctx {
 
 static size_t ncell(const mhd_ctx* c) { return (size_t)c->nx * c->ny * c->nz; }
 
+// Bulk-TMA rules for x-pencils of the context's element type (the state
+// buffers come from cudaMalloc and are 256-byte aligned).
+static int tma_ok(const mhd_ctx* c, int nx)
+{
+    return ((size_t)nx * 5 * c->elem) % 16 == 0 && ((size_t)nx * 3 * c->elem) % 16 == 0;
+}
+
+// CFL partials written by the epilogue of the step's last fluidx.
+static size_t fluidx_parts(const mhd_ctx* c)
+{
+    return (size_t)c->ks->fluidx_parts(c->nx, c->ny, c->nz, tma_ok(c, c->nx));
+}
+
 static cudaEvent_t ev_get(mhd_ctx* c)
 {
     if (!c->ev_free.empty()) {
@@ -515,7 +528,7 @@ extern "C" MHD_API int mhd_set_state(mhd_ctx* c, const void* u, const void* b, i
     // epilogue), allocated here so a captured step never reallocates.
     {
         const size_t a = (ncell(c) + 255) / 256;
-        const size_t f = (size_t)(c->ny / fluidx_pencils(c->nx, c->ny)) * c->nz;
+        const size_t f = fluidx_parts(c);
         MHD_TRY(set_err(c->part.ensure(((a > f ? a : f) + 1) * c->ks->part_bytes)));
     }
     (void)where;  // direction inferred from the pointers (unified addressing)
@@ -622,7 +635,7 @@ static int enqueue_plain_step(mhd_ctx* c, double cfl)
     MHD_TRY(op_transpose(c, 1, U1, B1, U0, B0, ny, nx, nz));
     MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt));
     // last fluidx with the calcfl epilogue for the next step
-    const size_t nparts = (size_t)(ny / fluidx_pencils(nx, ny)) * nz;
+    const size_t nparts = fluidx_parts(c);
     if (c->part.cap < nparts * c->ks->part_bytes)  // sized by mhd_set_state
         return MHD_ERR_ARG;
     MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, c->part.p));
@@ -656,8 +669,7 @@ static int step_graph(mhd_ctx* c, double cfl, int variant)
     MHD_TRY(ensure_cfl(c));
     // The graph's first node (finalize) reads cfl_nparts partials; those are
     // written by the previous step's last fluidx, whose grid does not change.
-    const FluidxArgs probe{nullptr, nullptr, nullptr, c->nx, c->ny, c->nz, fluidx_pencils(c->nx, c->ny)};
-    const int steady = (c->ny / probe.P) * c->nz;
+    const int steady = (int)fluidx_parts(c);
     if (c->cfl_nparts != steady)  // first step after a standalone calcfl
         return step_once_direct(c, cfl, variant);
     if (!c->gexec[variant] || c->gcfl[variant] != cfl) {

@@ -1,0 +1,282 @@
+// advectbyzx with C cells per thread (C/advectbyzx.c:14-23, A1
+// C/advectbyzxA1.c:18-63, A2 C/advectbyzxA2.c:9-28, B1 C/advectbyzxB1.c:19-62,
+// B2 C/advectbyzxB2.c:9-28, tvdb C/tvdb.c:10-91).
+//
+// A CTA owns P consecutive pencils (j0..j0+P-1, k) and computes 3P+1 tvdb
+// rows: A rows for pencils j0..j0+P at plane k (b(2) advected with the face
+// velocity of pencils j-1, j) and B rows for pencils j0..j0+P-1 at planes k
+// and k+1 (b(3) with pencils k-1, k).  Every row is owned by T = n/C threads
+// holding C consecutive cells; the tvdb stencil moves between threads by
+// shuffles.  The per-cell EMFs of the neighbour rows meet in shared memory and
+// the A-row threads of each owned pencil apply the float updates in the order
+// of A1, A2, B1, B2:
+//   b1_out = (((b1 - FA(j,k)) + FA(j+1,k)) - FB(j,k)) + FB(j,k+1).
+#pragma once
+#include "mhd_kernels.cuh"
+#include "mhd_pencil.cuh"
+
+namespace mhd {
+
+// Global chunk loads/stores of NF consecutive values with the widest vector
+// the alignment allows (the caller guarantees it: 16 B for NF % 4 == 0, 8 B
+// for NF % 2 == 0).
+template <typename R, int NF>
+__device__ __forceinline__ void ldg_chunk(const R* src, R (&dst)[NF])
+{
+    if constexpr (sizeof(R) == 4 && NF % 4 == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+        for (int v = 0; v < NF / 4; v++) {
+            const float4 x = __ldg(s4 + v);
+            dst[4 * v] = x.x;
+            dst[4 * v + 1] = x.y;
+            dst[4 * v + 2] = x.z;
+            dst[4 * v + 3] = x.w;
+        }
+    } else if constexpr (sizeof(R) == 4 && NF % 2 == 0) {
+        const float2* s2 = reinterpret_cast<const float2*>(src);
+#pragma unroll
+        for (int v = 0; v < NF / 2; v++) {
+            const float2 x = __ldg(s2 + v);
+            dst[2 * v] = x.x;
+            dst[2 * v + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NF; v++)
+            dst[v] = src[v];
+    }
+}
+
+template <typename R, int NF>
+__device__ __forceinline__ void stg_chunk(R* dst, const R (&src)[NF])
+{
+    if constexpr (sizeof(R) == 4 && NF % 4 == 0) {
+        float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+        for (int v = 0; v < NF / 4; v++)
+            d4[v] = make_float4(src[4 * v], src[4 * v + 1], src[4 * v + 2], src[4 * v + 3]);
+    } else if constexpr (sizeof(R) == 4 && NF % 2 == 0) {
+        float2* d2 = reinterpret_cast<float2*>(dst);
+#pragma unroll
+        for (int v = 0; v < NF / 2; v++)
+            d2[v] = make_float2(src[2 * v], src[2 * v + 1]);
+    } else {
+#pragma unroll
+        for (int v = 0; v < NF; v++)
+            dst[v] = src[v];
+    }
+}
+
+__host__ __device__ inline int advect2_rows(int P) { return 3 * P + 1; }
+
+// rows padded so that rows*T is a whole number of warps
+__host__ __device__ inline int advect2_threads(int P, int T)
+{
+    const int t = advect2_rows(P) * T;
+    return ((t + 31) / 32) * 32;
+}
+
+// shared memory (elements of R): FX [rows][n] + BN of the B rows at k [P][n] + seam
+__host__ __device__ inline size_t advect2_smem_elems(int n, int P)
+{
+    return (size_t)(advect2_rows(P) + P) * n + 2 * 32 * kSeamVals;
+}
+
+template <typename R, bool EX, int C, int T>
+__global__ void __launch_bounds__(512) k_advect2(AdvectArgs a)
+{
+    using W = wide_t<R, EX>;
+    constexpr int n = C * T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int P = a.P;
+    const int NR = advect2_rows(P);
+    const int tid = threadIdx.x;
+    const Group<R, T> g(tid);
+    int r = tid / T;
+    const bool live = r < NR;  // padding rows compute row 0 again and write nothing
+    if (!live)
+        r = 0;
+    const int i0 = g.t * C;
+    const int ny = a.ny, nz = a.nz;
+    const int j0 = blockIdx.x * P, k = blockIdx.y;
+    const int kp = (k + 1 == nz) ? 0 : k + 1;
+
+    R* FXs = reinterpret_cast<R*>(smem_raw);  // [NR][n]: F(i) = flux(i-1) of each row
+    R* BNs = FXs + (size_t)NR * n;            // [P][n]: advected b(3) of the B rows at k
+    R* seam = BNs + (size_t)P * n;
+
+    const R* uu = static_cast<const R*>(a.uu);
+    const R* ub = static_cast<const R*>(a.ub);
+    const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
+
+    // the two u pencils and the advected component of this row
+    size_t pm, pc;
+    int comp;
+    if (r <= P) {
+        int j = j0 + r;
+        if (j >= ny)
+            j -= ny;
+        const int jm = (j == 0) ? ny - 1 : j - 1;
+        pm = ((size_t)k * ny + jm) * n;
+        pc = ((size_t)k * ny + j) * n;
+        comp = 1;
+    } else {
+        const int r2 = r - (P + 1);
+        const int p = (r2 < P) ? r2 : r2 - P;
+        const int kk = (r2 < P) ? k : kp;
+        const int kkm = (kk == 0) ? nz - 1 : kk - 1;
+        pm = ((size_t)kkm * ny + j0 + p) * n;
+        pc = ((size_t)kk * ny + j0 + p) * n;
+        comp = 2;
+    }
+
+    // ---- raw face velocity (C/advectbyzxA1.c:31-35) and the advected field
+    R vr[C], bv[C], b1own[C];
+    {
+        R um[C * 5], uc[C * 5], bb[C * 3];
+        ldg_chunk<R, C * 5>(uu + (pm + i0) * 5, um);
+        ldg_chunk<R, C * 5>(uu + (pc + i0) * 5, uc);
+        ldg_chunk<R, C * 3>(ub + (pc + i0) * 3, bb);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R num = um[5 * m + 1] + uc[5 * m + 1], den = um[5 * m] + uc[5 * m];
+            if constexpr (EX)
+                vr[m] = num / den;
+            else
+                vr[m] = fast_div(num, den);
+            bv[m] = (comp == 1) ? bb[3 * m + 1] : bb[3 * m + 2];
+            b1own[m] = bb[3 * m];
+        }
+    }
+    // ---- 1-2-1 smoothing (C/advectbyzxA1.c:36-41)
+    R vg[C];
+    {
+        R l[1], rr[1], x0[1] = {vr[C - 1]}, x1[1] = {vr[0]};
+        g.template shift<1>(x0, l, -1, seam, 0);
+        g.template shift<1>(x1, rr, +1, seam, 1);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R vm = (m > 0) ? vr[m - 1] : l[0];
+            const R vp = (m + 1 < C) ? vr[m + 1] : rr[0];
+            if constexpr (EX)
+                vg[m] = R((W(vm + vp) + W(2.0) * W(vr[m])) / W(4.0));
+            else
+                vg[m] = ((vm + vp) + R(2) * vr[m]) * R(0.25);
+        }
+    }
+    // ---- tvdb half step (C/tvdb.c:25-52)
+    R vh[C], b1[C];
+    {
+        R t2[C];
+#pragma unroll
+        for (int m = 0; m < C; m++)
+            t2[m] = bv[m] * vg[m];
+        R xs[2] = {vg[0], t2[0]}, xr[2];
+        g.template shift<2>(xs, xr, +1, seam, 0);
+        R f1[C];
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R vgn = (m + 1 < C) ? vg[m + 1] : xr[0];
+            const R t2n = (m + 1 < C) ? t2[m + 1] : xr[1];
+            vh[m] = lin<R, EX>(R(0.5), vg[m], R(0.5), vgn);
+            f1[m] = (vh[m] > R(0)) ? t2[m] : t2n;
+        }
+        R fl[1], fx[1] = {f1[C - 1]};
+        g.template shift<1>(fx, fl, -1, seam, 1);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R fm = (m > 0) ? f1[m - 1] : fl[0];
+            if constexpr (EX)
+                b1[m] = R(W(bv[m]) - W((f1[m] - fm) * dt) / W(2.0));
+            else
+                b1[m] = bv[m] - (f1[m] - fm) * dt * R(0.5);
+        }
+    }
+    // ---- limited upwind flux (C/tvdb.c:54-78)
+    R flux[C];
+    {
+        R vb[C];
+#pragma unroll
+        for (int m = 0; m < C; m++)
+            vb[m] = vg[m] * b1[m];
+        R l[1], x0[1] = {vb[C - 1]};
+        g.template shift<1>(x0, l, -1, seam, 0);
+        R xs[2] = {vb[0], vb[1 < C ? 1 : 0]}, xr[2];
+        g.template shift<2>(xs, xr, +1, seam, 1);
+        // right neighbour's first two values; for C == 1 the second is two threads away
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R vbm = (m > 0) ? vb[m - 1] : l[0];
+            const R vbp = (m + 1 < C) ? vb[m + 1] : xr[0];
+            const R vbpp = (m + 2 < C) ? vb[m + 2] : ((m + 2 == C) ? xr[0] : xr[1]);
+            R w, wp, wm;
+            if (vh[m] > R(0)) {
+                w = vb[m];
+                wp = R(W(vbp - w) / W(2.0));
+                wm = R(W(w - vbm) / W(2.0));
+            } else {
+                w = vbp;
+                wp = R(W(w - vbpp) / W(2.0));
+                wm = R(W(vb[m] - w) / W(2.0));
+            }
+            const R dw = vanleer<R, EX>(wm, wp);
+            flux[m] = (w + dw) * dt;
+        }
+    }
+    // ---- b - (flux - flux(i-1)) (C/tvdb.c:79-88) and F(i) = flux(i-1)
+    R bnew[C], F[C];
+    {
+        R l[1], x0[1] = {flux[C - 1]};
+        g.template shift<1>(x0, l, -1, seam, 0);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            F[m] = (m > 0) ? flux[m - 1] : l[0];
+            bnew[m] = bv[m] - (flux[m] - F[m]);
+        }
+    }
+    if (live) {
+        R* fx = FXs + (size_t)r * n + i0;
+#pragma unroll
+        for (int m = 0; m < C; m++)
+            fx[m] = F[m];
+        if (r > P && r <= 2 * P) {
+            R* bn = BNs + (size_t)(r - P - 1) * n + i0;
+#pragma unroll
+            for (int m = 0; m < C; m++)
+                bn[m] = bnew[m];
+        }
+    }
+    __syncthreads();
+    // ---- A1/A2/B1/B2 combine by the A-row threads of the owned pencils
+    if (live && r < P) {
+        const size_t cell0 = pc + i0;  // pencil (j0+r, k)
+        const R* b1s = static_cast<const R*>(a.b1_src);
+        if (b1s != ub) {
+            R bb[C * 3];
+            ldg_chunk<R, C * 3>(b1s + cell0 * 3, bb);
+#pragma unroll
+            for (int m = 0; m < C; m++)
+                b1own[m] = bb[3 * m];
+        }
+        R out[C * 3];
+        const R* fa1 = FXs + (size_t)(r + 1) * n + i0;
+        const R* fb = FXs + (size_t)(P + 1 + r) * n + i0;
+        const R* fbp = FXs + (size_t)(2 * P + 1 + r) * n + i0;
+        const R* b3 = BNs + (size_t)r * n + i0;
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            R x = b1own[m];
+            x = x - F[m];
+            x = x + fa1[m];
+            x = x - fb[m];
+            x = x + fbp[m];
+            out[3 * m] = x;
+            out[3 * m + 1] = bnew[m];
+            out[3 * m + 2] = b3[m];
+        }
+        stg_chunk<R, C * 3>(static_cast<R*>(a.b_out) + cell0 * 3, out);
+    }
+}
+
+}  // namespace mhd

@@ -1,0 +1,279 @@
+// fluidx with C cells per thread (C/fluidx.c:19-102, C/tvd1.c:8-118,
+// C/mhdflux.c:9-72).  A CTA stages P consecutive x-pencils of u and the b
+// pencils at (j..j+P, k) and (j.., kp) into shared memory with bulk TMA, each
+// pencil is owned by T = n/C threads (mhd_pencil.cuh), and the relaxing TVD
+// update runs in registers: the two pencil maxima are shuffle reductions and
+// the five neighbour exchanges of the stencil are shuffles.  The new u goes
+// back through shared memory and one bulk TMA store.
+#pragma once
+#include "mhd_kernels.cuh"
+#include "mhd_pencil.cuh"
+
+namespace mhd {
+
+template <int C, int T>
+struct Fx2Shape {
+    static constexpr int N = C * T;  // cells per pencil
+};
+
+// shared memory (elements of R): su 5nP, sb 3n(P+1), sbk 3nP, red 32, seam 2*32*10
+__host__ __device__ inline size_t fluidx2_smem_elems(int n, int P)
+{
+    const size_t np = (size_t)n * P;
+    return 5 * np + 3 * (np + n) + 3 * np + 32 + 2 * 32 * 10;
+}
+
+template <typename R, bool EX, int C, int T>
+__global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
+{
+    constexpr int n = C * T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int P = a.P;
+    const int np = n * P;
+    const int tid = threadIdx.x;
+    const int lp = tid / T;  // local pencil
+    const Group<R, T> g(tid);
+    const int i0 = g.t * C;
+    const int j0 = blockIdx.x * P, k = blockIdx.y;
+    const int kp = (k + 1 == a.nz) ? 0 : k + 1;
+    const int jn = (j0 + P == a.ny) ? 0 : j0 + P;
+
+    R* su = reinterpret_cast<R*>(smem_raw);
+    R* sb = su + 5 * np;
+    R* sbk = sb + 3 * (np + n);
+    R* red = sbk + 3 * np;
+    R* seam = red + 32;
+    __shared__ uint64_t bar;
+
+    const R* uu = static_cast<const R*>(a.uu);
+    const R* ub = static_cast<const R*>(a.ub);
+    const size_t c0 = ((size_t)k * a.ny + j0) * n;
+    const size_t cn = ((size_t)k * a.ny + jn) * n;
+    const size_t ck = ((size_t)kp * a.ny + j0) * n;
+
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        const uint32_t bu = 5u * np * sizeof(R), bg = 3u * np * sizeof(R), b1 = 3u * n * sizeof(R);
+        mbar_arrive_expect_tx(&bar, bu + 2 * bg + b1);
+        tma_load_1d(su, uu + c0 * 5, bu, &bar);
+        tma_load_1d(sb, ub + c0 * 3, bg, &bar);
+        tma_load_1d(sb + 3 * np, ub + cn * 3, b1, &bar);
+        tma_load_1d(sbk, ub + ck * 3, bg, &bar);
+    }
+    __syncthreads();
+    mbar_wait_bounded(&bar, 0, a.err);
+
+    const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
+    using W = wide_t<R, EX>;
+
+    // ---- gather this thread's cells
+    R q[C][5], f[C][3];
+    {
+        R qf[C * 5], bjf[C * 3], bpf[C * 3], bkf[C * 3];
+        lds_chunk<R, C * 5>(su + (size_t)(lp * n + i0) * 5, qf);
+        const R* bj = sb + (size_t)(lp * n) * 3;
+        lds_chunk<R, C * 3>(bj + 3 * i0, bjf);
+        lds_chunk<R, C * 3>(sb + (size_t)((lp + 1) * n + i0) * 3, bpf);
+        lds_chunk<R, C * 3>(sbk + (size_t)(lp * n + i0) * 3, bkf);
+        const int inext = (i0 + C == n) ? 0 : i0 + C;
+        const R b1next = bj[3 * inext];
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+#pragma unroll
+            for (int s = 0; s < 5; s++)
+                q[m][s] = qf[5 * m + s];
+            const R h0 = R(0.5) * bjf[3 * m];
+            const R h0p = R(0.5) * ((m + 1 < C) ? bjf[3 * (m + 1)] : b1next);
+            f[m][0] = h0 + h0p;                                        // C/fluidx.c:71-78
+            f[m][1] = R(0.5) * bjf[3 * m + 1] + bpf[3 * m + 1] / R(2);  // C/fluidx.c:79
+            f[m][2] = R(0.5) * bjf[3 * m + 2] + bkf[3 * m + 2] / R(2);  // C/fluidx.c:80
+        }
+    }
+
+    // ---- stage 1 (C/tvd1.c:33-49)
+    R fr[C][5], gl[C][5];  // fr = c*wr, gl = c*wl (so fl(i) = gl(i+1))
+    {
+        R v[C][5], cmax = R(0);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            R ci;
+            cell_flux<R, EX>(q[m], f[m], v[m], ci);
+            cmax = fmax(cmax, ci);
+        }
+        const R c = g.max(cmax, red);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            if constexpr (EX) {
+                scale_flux<R, EX>(v[m], c);
+#pragma unroll
+                for (int s = 0; s < 5; s++) {
+                    fr[m][s] = scale0<R, EX>(c, lin<R, EX>(R(1), q[m][s], R(1), v[m][s]));
+                    gl[m][s] = scale0<R, EX>(c, lin<R, EX>(R(1), q[m][s], R(-1), v[m][s]));
+                }
+            } else {
+                // c*(u +- v/c) = c*u +- v when c > 0; both vanish when c == 0
+                const bool pos = c > R(0);
+#pragma unroll
+                for (int s = 0; s < 5; s++) {
+                    fr[m][s] = pos ? fma(c, q[m][s], v[m][s]) : R(0);
+                    gl[m][s] = pos ? fma(c, q[m][s], -v[m][s]) : R(0);
+                }
+            }
+        }
+    }
+    R u1[C][5];
+    {
+        R gnext[5], flux[C][5];
+        g.template shift<5>(gl[0], gnext, +1, seam, 0);
+#pragma unroll
+        for (int m = 0; m < C; m++)
+#pragma unroll
+            for (int s = 0; s < 5; s++)
+                flux[m][s] = lin<R, EX>(R(0.5), fr[m][s], R(-0.5), (m + 1 < C) ? gl[m + 1][s] : gnext[s]);
+        R fprev[5];
+        g.template shift<5>(flux[C - 1], fprev, -1, seam, 1);
+        const R hdt = R(W(-1.0) * W(dt) / W(2.0));
+#pragma unroll
+        for (int m = 0; m < C; m++)
+#pragma unroll
+            for (int s = 0; s < 5; s++)
+                u1[m][s] = lin<R, EX>(R(1), q[m][s], hdt,
+                                      lin<R, EX>(R(1), flux[m][s], R(-1), (m > 0) ? flux[m - 1][s] : fprev[s]));
+    }
+
+    // ---- stage 2 (C/tvd1.c:51-116)
+    {
+        R v[C][5], cmax = R(0);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            R ci;
+            cell_flux<R, EX>(u1[m], f[m], v[m], ci);
+            cmax = fmax(cmax, ci);
+        }
+        const R c = g.max(cmax, red + 16);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            if constexpr (EX) {
+                scale_flux<R, EX>(v[m], c);
+#pragma unroll
+                for (int s = 0; s < 5; s++) {
+                    fr[m][s] = scale0<R, EX>(c, lin<R, EX>(R(1), u1[m][s], R(1), v[m][s]));
+                    gl[m][s] = scale0<R, EX>(c, lin<R, EX>(R(1), u1[m][s], R(-1), v[m][s]));
+                }
+            } else {
+                const bool pos = c > R(0);
+#pragma unroll
+                for (int s = 0; s < 5; s++) {
+                    fr[m][s] = pos ? fma(c, u1[m][s], v[m][s]) : R(0);
+                    gl[m][s] = pos ? fma(c, u1[m][s], -v[m][s]) : R(0);
+                }
+            }
+        }
+    }
+    R flux[C][5];
+    {
+        R xs[10], xr[10];
+        // left neighbour's last fr, right neighbour's first gl (fl(i) = gl(i+1))
+        R frp[5], gln[5];
+        g.template shift<5>(fr[C - 1], frp, -1, seam, 0);
+        g.template shift<5>(gl[0], gln, +1, seam, 1);
+        R dm[C][5], dl[C][5];  // dfrm(i), dflm(i)
+#pragma unroll
+        for (int m = 0; m < C; m++)
+#pragma unroll
+            for (int s = 0; s < 5; s++) {
+                dm[m][s] = lin<R, EX>(R(0.5), fr[m][s], R(-0.5), (m > 0) ? fr[m - 1][s] : frp[s]);
+                dl[m][s] = lin<R, EX>(R(0.5), gl[m][s], R(-0.5), (m + 1 < C) ? gl[m + 1][s] : gln[s]);
+            }
+#pragma unroll
+        for (int s = 0; s < 5; s++) {
+            xs[s] = dm[0][s];
+            xs[5 + s] = dl[0][s];
+        }
+        g.template shift<10>(xs, xr, +1, seam, 0);  // dfrp(i) = dfrm(i+1), dflp(i) = dflm(i+1)
+#pragma unroll
+        for (int m = 0; m < C; m++)
+#pragma unroll
+            for (int s = 0; s < 5; s++) {
+                const R dmn = (m + 1 < C) ? dm[m + 1][s] : xr[s];
+                const R dln = (m + 1 < C) ? dl[m + 1][s] : xr[5 + s];
+                R dfr, dfl;
+                if constexpr (EX) {
+                    dfr = vanleer<R, EX>(dmn, dm[m][s]);
+                    dfl = vanleer<R, EX>(dln, dl[m][s]);
+                } else {
+                    const R pr = dmn * dm[m][s], pl = dln * dl[m][s];
+                    dfr = (pr > R(0)) ? fast_div(R(2) * pr, dmn + dm[m][s]) : R(0);
+                    dfl = (pl > R(0)) ? fast_div(R(2) * pl, dln + dl[m][s]) : R(0);
+                }
+                const R gn = (m + 1 < C) ? gl[m + 1][s] : gln[s];
+                flux[m][s] = lin<R, EX>(R(0.5), lin<R, EX>(R(1), fr[m][s], R(-1), gn), R(0.5),
+                                        lin<R, EX>(R(1), dfr, R(-1), dfl));
+            }
+    }
+    {
+        R fprev[5];
+        g.template shift<5>(flux[C - 1], fprev, -1, seam, 1);
+        const R mdt = R(W(-1.0) * W(dt));
+        R of[C * 5];
+#pragma unroll
+        for (int m = 0; m < C; m++)
+#pragma unroll
+            for (int s = 0; s < 5; s++) {
+                q[m][s] = lin<R, EX>(R(1), q[m][s], mdt,
+                                     lin<R, EX>(R(1), flux[m][s], R(-1), (m > 0) ? flux[m - 1][s] : fprev[s]));
+                of[5 * m + s] = q[m][s];
+            }
+        // own cells: no other thread reads them after the gather
+        sts_chunk<R, C * 5>(su + (size_t)(lp * n + i0) * 5, of);
+    }
+
+    // ---- optional calcfl epilogue on the new state (face b at (j,k))
+    if (a.cfl_part) {
+        const R* bj = sb + (size_t)(lp * n + i0) * 3;
+        R m = R(0);
+        int ln = -1;
+#pragma unroll
+        for (int mm = 0; mm < C; mm++) {
+            const R fc[3] = {bj[3 * mm], bj[3 * mm + 1], bj[3 * mm + 2]};
+            const R sp = cfl_speed<R, EX>(q[mm], fc);
+            if (sp != sp)
+                ln = (int)(c0 + lp * n + i0 + mm);
+            else
+                m = fmax(m, sp);
+        }
+        m = warp_max<R>(m);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            ln = max(ln, __shfl_xor_sync(kFull, ln, o));
+        __syncthreads();  // red is reused below
+        int* rn = reinterpret_cast<int*>(seam);
+        if ((tid & 31) == 0) {
+            red[tid >> 5] = m;
+            rn[tid >> 5] = ln;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            R cm = R(0);
+            int lnan = -1;
+            for (int s = 0; s < (int)(blockDim.x >> 5); s++) {
+                cm = fmax(cm, red[s]);
+                lnan = max(lnan, rn[s]);
+            }
+            CflPart<R>* part = static_cast<CflPart<R>*>(a.cfl_part) + (blockIdx.y * gridDim.x + blockIdx.x);
+            part->cmax = cm;
+            part->last_nan = lnan;
+        }
+    }
+
+    // ---- write the new pencils
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+        tma_store_1d(static_cast<R*>(a.u_out) + c0 * 5, su, 5u * np * sizeof(R));
+        tma_store_commit();
+        tma_store_wait_all();
+    }
+}
+
+}  // namespace mhd

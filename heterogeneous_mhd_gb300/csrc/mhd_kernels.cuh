@@ -509,6 +509,25 @@ __global__ void __launch_bounds__(512) k_advect(AdvectArgs a)
 
 // -------------------------------------------------------------- transposes
 
+// Component permutations: transpose12 takes u components (1,3,2,4,5) and b
+// components (2,1,3) (C/transpose12.c:22-29); transpose13 takes u (1,4,3,2,5)
+// and b (3,2,1) (C/transpose13.c:24-31).  Written as selects so no lookup
+// table lands in local memory.
+template <int AXIS>
+__host__ __device__ __forceinline__ int perm_u(int c)
+{
+    if (AXIS == 1)
+        return (c == 1) ? 2 : (c == 2) ? 1 : c;
+    return (c == 1) ? 3 : (c == 3) ? 1 : c;
+}
+template <int AXIS>
+__host__ __device__ __forceinline__ int perm_b(int c)
+{
+    if (AXIS == 1)
+        return (c < 2) ? 1 - c : c;
+    return 2 - c;
+}
+
 // Transpose tile edge in cells: 32 for float, 16 for double (static shared
 // memory stays under 48 KB).
 template <typename R>
@@ -548,20 +567,18 @@ __global__ void __launch_bounds__(256) k_transpose(TransposeArgs a)
     }
     __syncthreads();
     // output: axis 1 -> dims (ny,nx,nz), cell (a, i, z); axis 2 -> dims (nz,ny,nx), cell (a, z, i)
-    const int pu1[5] = {0, 2, 1, 3, 4}, pb1[3] = {1, 0, 2};
-    const int pu2[5] = {0, 3, 2, 1, 4}, pb2[3] = {2, 1, 0};
     for (int r = 0; r < ti; r++) {
         const int iv = i0 + r;
         const size_t cout = (a.axis == 1) ? (((size_t)z * nx + iv) * ny + a0)
                                           : (((size_t)iv * ny + z) * nz + a0);
         for (int e = threadIdx.x; e < ta * 5; e += blockDim.x) {
             const int aa = e / 5, c = e - aa * 5;
-            const int src = (a.axis == 1) ? pu1[c] : pu2[c];
+            const int src = (a.axis == 1) ? perm_u<1>(c) : perm_u<2>(c);
             uo[cout * 5 + e] = su[aa][r * 5 + src];
         }
         for (int e = threadIdx.x; e < ta * 3; e += blockDim.x) {
             const int aa = e / 3, c = e - aa * 3;
-            const int src = (a.axis == 1) ? pb1[c] : pb2[c];
+            const int src = (a.axis == 1) ? perm_b<1>(c) : perm_b<2>(c);
             bo[cout * 3 + e] = sb[aa][r * 3 + src];
         }
     }

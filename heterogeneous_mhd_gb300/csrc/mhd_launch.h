@@ -20,6 +20,8 @@ struct KernelSet {
     cudaError_t (*cfl_finalize)(const CflFinalizeArgs&, cudaStream_t);
     cudaError_t (*divb)(const void* b, int nx, int ny, int nz, double* part, int* nparts, cudaStream_t);
     size_t part_bytes; // sizeof(CflPart<R>)
+    // number of CTAs (= CFL partials of the epilogue) of a fluidx launch
+    int (*fluidx_parts)(int nx, int ny, int nz, int aligned);
 };
 
 const KernelSet* kernels_f32_fast();

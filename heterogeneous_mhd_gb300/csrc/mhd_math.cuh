@@ -31,6 +31,41 @@ __device__ __forceinline__ float rabs<float>(float x)
     return fabsf(x);
 }
 
+// FAST-policy division, reciprocal and square root: the SFU approximations
+// (a few ulp) in FP32, IEEE in FP64.
+template <typename R>
+__device__ __forceinline__ R fast_rcp(R x)
+{
+    return R(1) / x;
+}
+template <>
+__device__ __forceinline__ float fast_rcp<float>(float x)
+{
+    return __fdividef(1.0f, x);
+}
+template <typename R>
+__device__ __forceinline__ R fast_div(R x, R y)
+{
+    return x / y;
+}
+template <>
+__device__ __forceinline__ float fast_div<float>(float x, float y)
+{
+    return __fdividef(x, y);
+}
+template <typename R>
+__device__ __forceinline__ R fast_sqrt(R x)
+{
+    return sqrt(x);
+}
+template <>
+__device__ __forceinline__ float fast_sqrt<float>(float x)
+{
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // abXYc_matrix2D with c = 0 (C/includefunc_spu.h:73-84): a*X + b*Y + 0.
 template <typename R, bool EX>
 __device__ __forceinline__ R lin(R a, R x, R b, R y)
@@ -62,7 +97,7 @@ __device__ __forceinline__ R vanleer(R a, R b)
         if constexpr (EX)
             r = R(W(2.0) * W(a) * W(b) / W(a + b));
         else
-            r = R(2) * a * b / (a + b);
+            r = fast_div(R(2) * a * b, a + b);
     }
     return r;
 }
@@ -88,7 +123,7 @@ __device__ __forceinline__ void cell_flux(const R q[5], const R f[3], R v[5], R&
         R p = R(W(ps) - W(bb) / W(2.0));
         ci = R(fabs(W(vx)) + sqrt(fabs(W((bb + gamma * p) / q[0]))));
     } else {
-        const R ri = R(1) / q[0];
+        const R ri = fast_rcp(q[0]);
         const R vx = q[1] * ri;
         const R mm = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
         const R bb = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
@@ -99,7 +134,7 @@ __device__ __forceinline__ void cell_flux(const R q[5], const R f[3], R v[5], R&
         v[3] = q[3] * vx - f[2] * f[0];
         v[4] = (q[4] + ps) * vx - f[0] * (f[0] * q[1] + f[1] * q[2] + f[2] * q[3]) * ri;
         const R p = ps - R(0.5) * bb;
-        ci = rabs(vx) + sqrt(rabs((bb + gamma * p) * ri));
+        ci = rabs(vx) + fast_sqrt(rabs((bb + gamma * p) * ri));
     }
 }
 
@@ -113,7 +148,7 @@ __device__ __forceinline__ void scale_flux(R v[5], R c)
             for (int q = 0; q < 5; q++)
                 v[q] = v[q] / c;
         } else {
-            const R rc = R(1) / c;
+            const R rc = fast_rcp(c);
 #pragma unroll
             for (int q = 0; q < 5; q++)
                 v[q] = v[q] * rc;
@@ -148,13 +183,13 @@ __device__ __forceinline__ R cfl_speed(const R q[5], const R f[3])
         R p = R(W(ps) - W(bb) / W(2.0));
         return R(W(v) + sqrt(fabs(W(bb) * W(2.0) + W(gamma * p)) / W(q[0])));
     } else {
-        const R ri = R(1) / q[0];
+        const R ri = fast_rcp(q[0]);
         const R v = max3(rabs(q[1] * ri), rabs(q[2] * ri), rabs(q[3] * ri));
         const R mm = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
         const R bb = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
         const R ps = (q[4] - R(0.5) * mm * ri) * (gamma - R(1)) + R(0.5) * (R(2) - gamma) * bb;
         const R p = ps - R(0.5) * bb;
-        return v + sqrt(rabs(bb * R(2) + gamma * p) * ri);
+        return v + fast_sqrt(rabs(bb * R(2) + gamma * p) * ri);
     }
 }
 

@@ -1,0 +1,130 @@
+// Pencil engine: a pencil of n cells is owned by T = n/C threads, thread t
+// holding the C consecutive cells t*C .. t*C+C-1 in registers.  Neighbour
+// values across chunk boundaries move by warp shuffles; when a pencil spans
+// several warps (T > 32) the values at the warp seams go through shared
+// memory with one block barrier per exchange round.  The periodic wrap
+// (cell n-1 <-> cell 0) is the wrap of the thread index.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace mhd {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kSeamVals = 10;  // largest exchange (values per thread and round)
+
+// Contiguous chunk of NF values to/from shared memory; 128-bit accesses for
+// float when NF % 4 == 0 (the caller guarantees 16-byte alignment).
+template <typename R, int NF>
+__device__ __forceinline__ void lds_chunk(const R* src, R (&dst)[NF])
+{
+    if constexpr (sizeof(R) == 4 && NF % 4 == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+        for (int v = 0; v < NF / 4; v++) {
+            const float4 x = s4[v];
+            dst[4 * v] = x.x;
+            dst[4 * v + 1] = x.y;
+            dst[4 * v + 2] = x.z;
+            dst[4 * v + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NF; v++)
+            dst[v] = src[v];
+    }
+}
+
+template <typename R, int NF>
+__device__ __forceinline__ void sts_chunk(R* dst, const R (&src)[NF])
+{
+    if constexpr (sizeof(R) == 4 && NF % 4 == 0) {
+        float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+        for (int v = 0; v < NF / 4; v++)
+            d4[v] = make_float4(src[4 * v], src[4 * v + 1], src[4 * v + 2], src[4 * v + 3]);
+    } else {
+#pragma unroll
+        for (int v = 0; v < NF; v++)
+            dst[v] = src[v];
+    }
+}
+
+// Exchange helper for one group of T threads (T a power of two <= 32, or a
+// multiple of 32).  `seam` is this CTA's scratch for warp-seam values: two
+// alternating banks of [warps][kSeamVals] elements.
+template <typename R, int T>
+struct Group {
+    static constexpr bool kMulti = (T > 32);
+    static constexpr int kWarps = kMulti ? T / 32 : 1;
+    static_assert(T <= 32 ? ((T & (T - 1)) == 0) : (T % 32 == 0), "T must be a power of two <= 32 or a multiple of 32");
+
+    int t;       // thread index inside the group (0..T-1)
+    int lane;    // lane in the warp
+    int warp;    // warp index in the CTA
+    int gwarp0;  // first warp of this group in the CTA
+
+    __device__ __forceinline__ Group(int tid)
+    {
+        t = tid % T;
+        lane = tid & 31;
+        warp = tid >> 5;
+        gwarp0 = warp - (t >> 5);
+    }
+
+    // Max over the group's values (starting from 0, NaN skipped as by fmax).
+    __device__ __forceinline__ R max(R x, R* red) const
+    {
+        const int w = (T < 32) ? T : 32;
+#pragma unroll
+        for (int o = w / 2; o > 0; o >>= 1)
+            x = fmax(x, __shfl_xor_sync(kFull, x, o));
+        if constexpr (kMulti) {
+            if (lane == 0)
+                red[warp] = x;
+            __syncthreads();
+            R m = R(0);
+#pragma unroll
+            for (int s = 0; s < kWarps; s++)
+                m = fmax(m, red[gwarp0 + s]);
+            return m;
+        } else {
+            return fmax(R(0), x);
+        }
+    }
+
+    // out[k] = x[k] of the thread t+1 (dir = +1) or t-1 (dir = -1), periodic.
+    // For T > 32 one barrier; `bank` (0/1) must alternate between consecutive calls.
+    template <int K>
+    __device__ __forceinline__ void shift(const R (&x)[K], R (&out)[K], int dir, R* seam, int bank) const
+    {
+        if constexpr (!kMulti) {
+            const int src = (dir > 0) ? ((t + 1) & (T - 1)) : ((t + T - 1) & (T - 1));
+#pragma unroll
+            for (int k = 0; k < K; k++)
+                out[k] = __shfl_sync(kFull, x[k], src, T);
+        } else {
+            static_assert(K <= kSeamVals, "too many values per exchange");
+            R* s = seam + bank * (32 * kSeamVals);  // [warp][K], fixed bank stride
+            const int edge = (dir > 0) ? 0 : 31;     // the lane whose value crosses the seam
+            if (lane == edge) {
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    s[warp * K + k] = x[k];
+            }
+#pragma unroll
+            for (int k = 0; k < K; k++)
+                out[k] = (dir > 0) ? __shfl_down_sync(kFull, x[k], 1) : __shfl_up_sync(kFull, x[k], 1);
+            __syncthreads();
+            const int need = (dir > 0) ? 31 : 0;
+            if (lane == need) {
+                const int gw = warp - gwarp0;
+                const int nb = (dir > 0) ? ((gw + 1) % kWarps) : ((gw + kWarps - 1) % kWarps);
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    out[k] = s[(gwarp0 + nb) * K + k];
+            }
+        }
+    }
+};
+
+}  // namespace mhd
