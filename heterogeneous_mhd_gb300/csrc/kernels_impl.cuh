@@ -6,9 +6,11 @@
 // n = 8T, T in {4..64} or 6T, T in {8..64}; transposes: full 32x32 tiles) and
 // a general kernel for every other shape.  FP64 uses the general kernels.
 #include "mhd_advect2.cuh"
+#include "mhd_advect3.cuh"
 #include "mhd_fluidx2.cuh"
 #include "mhd_launch.h"
 #include "mhd_transpose2.cuh"
+#include "mhd_transpose3.cuh"
 
 namespace mhd {
 namespace MHD_SET_NAME {
@@ -18,9 +20,11 @@ constexpr bool EX = MHD_EXACT;
 constexpr bool kV2 = (sizeof(R) == 4);
 
 // Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum
-// minus its static shared memory (once per kernel).
+// minus its static shared memory (once per kernel).  Kernels that stage all
+// their input by TMA ask for the largest shared-memory carveout (they do not
+// use L1 for data), so residency is set by registers and shared memory only.
 template <typename K>
-static cudaError_t allow_smem(K kernel, bool& done)
+static cudaError_t allow_smem(K kernel, bool& done, bool tma_staged = false)
 {
     if (done)
         return cudaSuccess;
@@ -33,6 +37,8 @@ static cudaError_t allow_smem(K kernel, bool& done)
         e = cudaFuncGetAttributes(&fa, kernel);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess && tma_staged)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e == cudaSuccess)
         done = true;
     return e;
@@ -72,7 +78,7 @@ template <int C, int T>
 static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T>, attr);
+    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T>, attr, true);
     if (e != cudaSuccess)
         return e;
     dim3 grid(a.ny / a.P, a.nz);
@@ -142,6 +148,38 @@ static FxPlan plan_advect(int nx, int ny, bool aligned)
     return p;
 }
 
+// Marching kernel (C = 8, FP32): J pencils per CTA such that the slabs fit
+// two CTAs per SM, K planes per CTA such that there are >= 4 waves.
+static bool plan_advect3(int nx, int ny, int nz, bool aligned, int& T, int& J, int& K)
+{
+    if (!kV2 || !aligned || nx % 8 != 0 || !pow2_in(nx / 8, 4, 64))
+        return false;
+    T = nx / 8;
+    J = 0;
+    for (int j = 1; j <= ny && j <= 16; j++)
+        if (ny % j == 0 && advect3_threads(j, T) <= 384 && advect3_smem_floats(j, T) * 4 <= 113 * 1024)
+            J = j;
+    if (!J)
+        return false;
+    K = 1;
+    for (int k = 1; k <= nz && k <= 32; k++)
+        if (nz % k == 0 && (long long)(ny / J) * (nz / k) >= 4 * 2 * 152)
+            K = k;
+    return true;
+}
+
+template <int T>
+static cudaError_t launch_ad3(const AdvectArgs& a, cudaStream_t s)
+{
+    static bool attr = false;
+    cudaError_t e = allow_smem(k_advect3<EX, T>, attr, true);
+    if (e != cudaSuccess)
+        return e;
+    dim3 grid(a.ny / a.P, a.nz / a.K);
+    k_advect3<EX, T><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, T) * sizeof(float), s>>>(a);
+    return cudaGetLastError();
+}
+
 template <int C, int T>
 static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
 {
@@ -159,6 +197,20 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
     AdvectArgs a = in;
     const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
                          reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
+    if constexpr (kV2) {
+        int T3, J3, K3;
+        if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, T3, J3, K3)) {
+            a.P = J3;
+            a.K = K3;
+            switch (T3) {
+            case 4: return launch_ad3<4>(a, s);
+            case 8: return launch_ad3<8>(a, s);
+            case 16: return launch_ad3<16>(a, s);
+            case 32: return launch_ad3<32>(a, s);
+            case 64: return launch_ad3<64>(a, s);
+            }
+        }
+    }
     const FxPlan p = plan_advect(a.nx, a.ny, (al & 15) == 0);
     a.P = p.P;
     if constexpr (kV2) {
@@ -202,6 +254,14 @@ static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
     if constexpr (kV2) {
         const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.b_out) |
                              reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
+        if (a.nx % kT3 == 0 && na % kT3 == 0 && (al & 15) == 0) {  // bulk-TMA tiles
+            dim3 grid(a.nx / kT3, na / kT3, nb);
+            if (a.axis == 1)
+                k_transpose3<1><<<grid, 256, 0, s>>>(a);
+            else
+                k_transpose3<2><<<grid, 256, 0, s>>>(a);
+            return cudaGetLastError();
+        }
         if (a.nx % kT2 == 0 && na % kT2 == 0 && (al & 3) == 0) {
             dim3 grid(a.nx / kT2, na / kT2, nb);
             if (a.axis == 1)

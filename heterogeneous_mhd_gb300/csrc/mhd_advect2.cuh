@@ -68,6 +68,103 @@ __device__ __forceinline__ void stg_chunk(R* dst, const R (&src)[NF])
     }
 }
 
+// One tvdb row held by T threads with C cells each: from the raw face
+// velocity vr (C/advectbyzxA1.c:31-35) and the advected field bv, the 1-2-1
+// smoothing (C/advectbyzxA1.c:36-41) and tvdb (C/tvdb.c:10-91).  Returns
+// F(i) = flux(i-1) (the EMF times dt used by the CT update) and the advected
+// field.  Seven neighbour exchanges; for T > 32 each is one block barrier.
+template <typename R, bool EX, int C, int T>
+__device__ __forceinline__ void tvdb_row(const Group<R, T>& g, const R (&vr)[C], const R (&bv)[C], R dt, R* seam,
+                                         R (&F)[C], R (&bnew)[C])
+{
+    using W = wide_t<R, EX>;
+    // ---- 1-2-1 smoothing (C/advectbyzxA1.c:36-41)
+    R vg[C];
+    {
+        R l[1], rr[1], x0[1] = {vr[C - 1]}, x1[1] = {vr[0]};
+        g.template shift<1>(x0, l, -1, seam, 0);
+        g.template shift<1>(x1, rr, +1, seam, 1);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R vm = (m > 0) ? vr[m - 1] : l[0];
+            const R vp = (m + 1 < C) ? vr[m + 1] : rr[0];
+            if constexpr (EX)
+                vg[m] = R((W(vm + vp) + W(2.0) * W(vr[m])) / W(4.0));
+            else
+                vg[m] = ((vm + vp) + R(2) * vr[m]) * R(0.25);
+        }
+    }
+    // ---- tvdb half step (C/tvdb.c:25-52)
+    R vh[C], b1[C];
+    {
+        R t2[C];
+#pragma unroll
+        for (int m = 0; m < C; m++)
+            t2[m] = bv[m] * vg[m];
+        R xs[2] = {vg[0], t2[0]}, xr[2];
+        g.template shift<2>(xs, xr, +1, seam, 0);
+        R f1[C];
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R vgn = (m + 1 < C) ? vg[m + 1] : xr[0];
+            const R t2n = (m + 1 < C) ? t2[m + 1] : xr[1];
+            vh[m] = lin<R, EX>(R(0.5), vg[m], R(0.5), vgn);
+            f1[m] = (vh[m] > R(0)) ? t2[m] : t2n;
+        }
+        R fl[1], fx[1] = {f1[C - 1]};
+        g.template shift<1>(fx, fl, -1, seam, 1);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R fm = (m > 0) ? f1[m - 1] : fl[0];
+            if constexpr (EX)
+                b1[m] = R(W(bv[m]) - W((f1[m] - fm) * dt) / W(2.0));
+            else
+                b1[m] = bv[m] - (f1[m] - fm) * dt * R(0.5);
+        }
+    }
+    // ---- limited upwind flux (C/tvdb.c:54-78)
+    R flux[C];
+    {
+        R vb[C];
+#pragma unroll
+        for (int m = 0; m < C; m++)
+            vb[m] = vg[m] * b1[m];
+        R l[1], x0[1] = {vb[C - 1]};
+        g.template shift<1>(x0, l, -1, seam, 0);
+        R xs[2] = {vb[0], vb[1 < C ? 1 : 0]}, xr[2];
+        g.template shift<2>(xs, xr, +1, seam, 1);
+        // right neighbour's first two values; for C == 1 the second is two threads away
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const R vbm = (m > 0) ? vb[m - 1] : l[0];
+            const R vbp = (m + 1 < C) ? vb[m + 1] : xr[0];
+            const R vbpp = (m + 2 < C) ? vb[m + 2] : ((m + 2 == C) ? xr[0] : xr[1]);
+            R w, wp, wm;
+            if (vh[m] > R(0)) {
+                w = vb[m];
+                wp = R(W(vbp - w) / W(2.0));
+                wm = R(W(w - vbm) / W(2.0));
+            } else {
+                w = vbp;
+                wp = R(W(w - vbpp) / W(2.0));
+                wm = R(W(vb[m] - w) / W(2.0));
+            }
+            const R dw = vanleer<R, EX>(wm, wp);
+            flux[m] = (w + dw) * dt;
+        }
+    }
+    // ---- b - (flux - flux(i-1)) (C/tvdb.c:79-88) and F(i) = flux(i-1)
+    {
+        R l[1], x0[1] = {flux[C - 1]};
+        g.template shift<1>(x0, l, -1, seam, 0);
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            F[m] = (m > 0) ? flux[m - 1] : l[0];
+            bnew[m] = bv[m] - (flux[m] - F[m]);
+        }
+    }
+}
+
 __host__ __device__ inline int advect2_rows(int P) { return 3 * P + 1; }
 
 // rows padded so that rows*T is a whole number of warps
@@ -149,92 +246,8 @@ __global__ void __launch_bounds__(512) k_advect2(AdvectArgs a)
             b1own[m] = bb[3 * m];
         }
     }
-    // ---- 1-2-1 smoothing (C/advectbyzxA1.c:36-41)
-    R vg[C];
-    {
-        R l[1], rr[1], x0[1] = {vr[C - 1]}, x1[1] = {vr[0]};
-        g.template shift<1>(x0, l, -1, seam, 0);
-        g.template shift<1>(x1, rr, +1, seam, 1);
-#pragma unroll
-        for (int m = 0; m < C; m++) {
-            const R vm = (m > 0) ? vr[m - 1] : l[0];
-            const R vp = (m + 1 < C) ? vr[m + 1] : rr[0];
-            if constexpr (EX)
-                vg[m] = R((W(vm + vp) + W(2.0) * W(vr[m])) / W(4.0));
-            else
-                vg[m] = ((vm + vp) + R(2) * vr[m]) * R(0.25);
-        }
-    }
-    // ---- tvdb half step (C/tvdb.c:25-52)
-    R vh[C], b1[C];
-    {
-        R t2[C];
-#pragma unroll
-        for (int m = 0; m < C; m++)
-            t2[m] = bv[m] * vg[m];
-        R xs[2] = {vg[0], t2[0]}, xr[2];
-        g.template shift<2>(xs, xr, +1, seam, 0);
-        R f1[C];
-#pragma unroll
-        for (int m = 0; m < C; m++) {
-            const R vgn = (m + 1 < C) ? vg[m + 1] : xr[0];
-            const R t2n = (m + 1 < C) ? t2[m + 1] : xr[1];
-            vh[m] = lin<R, EX>(R(0.5), vg[m], R(0.5), vgn);
-            f1[m] = (vh[m] > R(0)) ? t2[m] : t2n;
-        }
-        R fl[1], fx[1] = {f1[C - 1]};
-        g.template shift<1>(fx, fl, -1, seam, 1);
-#pragma unroll
-        for (int m = 0; m < C; m++) {
-            const R fm = (m > 0) ? f1[m - 1] : fl[0];
-            if constexpr (EX)
-                b1[m] = R(W(bv[m]) - W((f1[m] - fm) * dt) / W(2.0));
-            else
-                b1[m] = bv[m] - (f1[m] - fm) * dt * R(0.5);
-        }
-    }
-    // ---- limited upwind flux (C/tvdb.c:54-78)
-    R flux[C];
-    {
-        R vb[C];
-#pragma unroll
-        for (int m = 0; m < C; m++)
-            vb[m] = vg[m] * b1[m];
-        R l[1], x0[1] = {vb[C - 1]};
-        g.template shift<1>(x0, l, -1, seam, 0);
-        R xs[2] = {vb[0], vb[1 < C ? 1 : 0]}, xr[2];
-        g.template shift<2>(xs, xr, +1, seam, 1);
-        // right neighbour's first two values; for C == 1 the second is two threads away
-#pragma unroll
-        for (int m = 0; m < C; m++) {
-            const R vbm = (m > 0) ? vb[m - 1] : l[0];
-            const R vbp = (m + 1 < C) ? vb[m + 1] : xr[0];
-            const R vbpp = (m + 2 < C) ? vb[m + 2] : ((m + 2 == C) ? xr[0] : xr[1]);
-            R w, wp, wm;
-            if (vh[m] > R(0)) {
-                w = vb[m];
-                wp = R(W(vbp - w) / W(2.0));
-                wm = R(W(w - vbm) / W(2.0));
-            } else {
-                w = vbp;
-                wp = R(W(w - vbpp) / W(2.0));
-                wm = R(W(vb[m] - w) / W(2.0));
-            }
-            const R dw = vanleer<R, EX>(wm, wp);
-            flux[m] = (w + dw) * dt;
-        }
-    }
-    // ---- b - (flux - flux(i-1)) (C/tvdb.c:79-88) and F(i) = flux(i-1)
     R bnew[C], F[C];
-    {
-        R l[1], x0[1] = {flux[C - 1]};
-        g.template shift<1>(x0, l, -1, seam, 0);
-#pragma unroll
-        for (int m = 0; m < C; m++) {
-            F[m] = (m > 0) ? flux[m - 1] : l[0];
-            bnew[m] = bv[m] - (flux[m] - F[m]);
-        }
-    }
+    tvdb_row<R, EX, C, T>(g, vr, bv, dt, seam, F, bnew);
     if (live) {
         R* fx = FXs + (size_t)r * n + i0;
 #pragma unroll

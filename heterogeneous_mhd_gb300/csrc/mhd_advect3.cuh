@@ -1,0 +1,241 @@
+// advectbyzx marching along k (C/advectbyzx.c:14-23 with A1/A2/B1/B2 and
+// tvdb, C/advectbyzxA1.c:18-63 ... C/tvdb.c:10-91).
+//
+// A CTA owns J consecutive pencils (j0..j0+J-1) and K consecutive planes
+// (k0..k0+K-1).  Marching k, it keeps a three-slot ring of plane slabs in
+// shared memory: u pencils j0-1..j0+J and b pencils j0..j0+J of one plane,
+// one bulk TMA copy per pencil (fewer, larger copies measured faster than
+// padded per-group copies that avoid the two-way bank conflicts of the
+// 40-word thread chunks).  The slab of plane k+2 is requested at the start of
+// step k, a whole step ahead of its use.  At step k the CTA computes
+//   * J+1 A rows at plane k   (b(2) advected with the face velocity of j-1, j),
+//   * J   B rows at plane k+1 (b(3) advected with the face velocity of k, k+1),
+// one row per thread group of T = n/C threads, and combines for each owned
+// pencil (the order of the float updates of A1, A2, B1, B2)
+//   b1_out = (((b1 - FA(j,k)) + FA(j+1,k)) - FB(j,k)) + FB(j,k+1)
+// with FB(.,k) and the advected b(3) of plane k kept from the previous step.
+// Every input pencil is read from global memory once per CTA and every B row
+// is computed once (one extra plane of B rows per K planes).
+#pragma once
+#include "mhd_advect2.cuh"
+
+namespace mhd {
+
+constexpr int kA3C = 8;             // cells per thread
+constexpr int kA3UW = kA3C * 5;     // u words per thread chunk
+constexpr int kA3BW = kA3C * 3;     // b words per thread chunk
+constexpr int kA3S = 3;             // ring slots
+
+__host__ __device__ inline int advect3_rows(int J) { return 2 * J + 1; }
+
+__host__ __device__ inline int advect3_threads(int J, int T)
+{
+    const int t = advect3_rows(J) * T;
+    return ((t + 31) / 32) * 32;
+}
+
+// shared memory in floats: 3 u slabs, 3 b slabs, FA[J+1][n], FB[2][J][n],
+// B3[2][J][n], seam; plus the mbarriers (in the static part)
+__host__ __device__ inline size_t advect3_smem_floats(int J, int T)
+{
+    const size_t uslab = (size_t)(J + 2) * T * kA3UW, bslab = (size_t)(J + 1) * T * kA3BW;
+    const size_t n = (size_t)T * kA3C;
+    return kA3S * uslab + kA3S * bslab + (J + 1) * n + 4 * J * n + 2 * 32 * kSeamVals;
+}
+
+template <bool EX, int T>
+__global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
+{
+    using R = float;
+    constexpr int C = kA3C;
+    constexpr int n = C * T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint64_t bar[kA3S];
+    const int J = a.P, K = a.K;
+    const int NR = advect3_rows(J);
+    const int tid = threadIdx.x;
+    const Group<R, T> g(tid);
+    int r = tid / T;
+    const bool live = r < NR;
+    if (!live)
+        r = 0;
+    const int ny = a.ny, nz = a.nz;
+    const int j0 = blockIdx.x * J, k0 = blockIdx.y * K;
+    const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
+
+    constexpr int UROW = T * kA3UW, BROW = T * kA3BW;  // words per pencil row
+    const size_t uslab = (size_t)(J + 2) * UROW, bslab = (size_t)(J + 1) * BROW;
+    float* U = reinterpret_cast<float*>(smem_raw);  // [3][J+2][n*5]
+    float* B = U + kA3S * uslab;                      // [3][J+1][n*3]
+    float* FA = B + kA3S * bslab;                     // [J+1][n]
+    float* FB = FA + (size_t)(J + 1) * n;             // [2][J][n]
+    float* B3 = FB + (size_t)2 * J * n;               // [2][J][n]
+    float* seam = B3 + (size_t)2 * J * n;
+
+    const float* uu = static_cast<const float*>(a.uu);
+    const float* ub = static_cast<const float*>(a.ub);
+
+    // ---- slab loads: plane p into ring slot s (one mbarrier per slot).
+    // Issued by warp 0: lane 0 registers the bytes, then one lane per pencil
+    // issues its bulk copy.
+    auto load_plane = [&](int p, int s) {
+        if (tid < 32) {
+            const int pp = ((p % nz) + nz) % nz;
+            if (tid == 0)
+                mbar_arrive_expect_tx(&bar[s], (uint32_t)((J + 2) * n * 20 + (J + 1) * n * 12));
+            __syncwarp();
+            for (int row = tid; row < J + 2; row += 32) {
+                int j = j0 - 1 + row;
+                j = (j < 0) ? j + ny : (j >= ny ? j - ny : j);
+                const size_t cell = ((size_t)pp * ny + j) * n;
+                tma_load_1d(U + s * uslab + (size_t)row * UROW, uu + cell * 5, n * 20, &bar[s]);
+            }
+            for (int row = tid; row < J + 1; row += 32) {
+                int j = j0 + row;
+                j = (j >= ny) ? j - ny : j;
+                const size_t cell = ((size_t)pp * ny + j) * n;
+                tma_load_1d(B + s * bslab + (size_t)row * BROW, ub + cell * 3, n * 12, &bar[s]);
+            }
+        }
+    };
+    // ring slot and mbarrier parity of plane p (slot 0 gets k0-1, k0+2, ...)
+    auto slot_of = [&](int p) { return (p - k0 + 1) % kA3S; };
+    auto parity_of = [&](int p) { return (uint32_t)(((p - k0 + 1) / kA3S) & 1); };
+
+    // this thread's chunk of u pencil `row` (0 = j0-1) / b pencil `row` (0 = j0) in slot s
+    auto u_chunk = [&](int s, int row, float (&out)[C * 5]) {
+        lds_chunk<float, C * 5>(U + s * uslab + (size_t)row * UROW + g.t * kA3UW, out);
+    };
+    auto b_chunk = [&](int s, int row, float (&out)[C * 3]) {
+        lds_chunk<float, C * 3>(B + s * bslab + (size_t)row * BROW + g.t * kA3BW, out);
+    };
+    // raw face velocity between two u chunks (C/advectbyzxA1.c:34, C/advectbyzxB1.c:34)
+    auto face_v = [&](const float (&um)[C * 5], const float (&uc)[C * 5], float (&vr)[C]) {
+#pragma unroll
+        for (int m = 0; m < C; m++) {
+            const float num = um[5 * m + 1] + uc[5 * m + 1], den = um[5 * m] + uc[5 * m];
+            if constexpr (EX)
+                vr[m] = num / den;
+            else
+                vr[m] = fast_div(num, den);
+        }
+    };
+
+    if (tid == 0)
+        for (int s = 0; s < kA3S; s++)
+            mbar_init(&bar[s], 1);
+    __syncthreads();
+    load_plane(k0 - 1, slot_of(k0 - 1));
+    load_plane(k0, slot_of(k0));
+    load_plane(k0 + 1, slot_of(k0 + 1));
+    mbar_wait_bounded(&bar[slot_of(k0 - 1)], parity_of(k0 - 1), a.err);
+    mbar_wait_bounded(&bar[slot_of(k0)], parity_of(k0), a.err);
+
+    // ---- prologue: B rows of plane k0 (FB and advected b(3) of the first step)
+    const bool brow = live && r > J;   // B-row groups: pencil j0 + (r-J-1)
+    const int bp = r - J - 1;
+    {
+        const int sm = slot_of(k0 - 1), sc = slot_of(k0);
+        float um[C * 5], uc[C * 5], bb[C * 3], vr[C], bv[C], F[C], bn[C];
+        const int prow = brow ? bp + 1 : 1;  // u row of pencil j0+bp
+        u_chunk(sm, prow, um);
+        u_chunk(sc, prow, uc);
+        b_chunk(sc, brow ? bp : 0, bb);
+        face_v(um, uc, vr);
+#pragma unroll
+        for (int m = 0; m < C; m++)
+            bv[m] = bb[3 * m + 2];
+        tvdb_row<R, EX, C, T>(g, vr, bv, dt, seam, F, bn);
+        if (brow) {
+            const int pb = k0 & 1;
+            float* fbw = FB + ((size_t)pb * J + bp) * n + g.t * C;
+            float* b3w = B3 + ((size_t)pb * J + bp) * n + g.t * C;
+#pragma unroll
+            for (int m = 0; m < C; m++) {
+                fbw[m] = F[m];
+                b3w[m] = bn[m];
+            }
+        }
+    }
+    __syncthreads();
+
+    const float* b1s = static_cast<const float*>(a.b1_src);
+    float* bo = static_cast<float*>(a.b_out);
+    for (int k = k0; k < k0 + K; k++) {
+        const int sk = slot_of(k), sk1 = slot_of(k + 1);
+        // plane k-1's slot is free (the previous step ended with a barrier)
+        if (k + 2 <= k0 + K) {
+            fence_proxy_async_smem();
+            load_plane(k + 2, slot_of(k + 2));
+        }
+        mbar_wait_bounded(&bar[sk1], parity_of(k + 1), a.err);
+        // ---- rows: A at plane k (r <= J), B at plane k+1 (r > J)
+        float F[C], bn[C], b1own[C];
+        {
+            float um[C * 5], uc[C * 5], bb[C * 3], vr[C], bv[C];
+            if (r <= J) {
+                u_chunk(sk, r, um);      // pencil j0+r-1
+                u_chunk(sk, r + 1, uc);  // pencil j0+r
+                b_chunk(sk, r, bb);
+            } else {
+                u_chunk(sk, bp + 1, um);   // plane k
+                u_chunk(sk1, bp + 1, uc);  // plane k+1
+                b_chunk(sk1, bp, bb);
+            }
+            face_v(um, uc, vr);
+#pragma unroll
+            for (int m = 0; m < C; m++) {
+                bv[m] = (r <= J) ? bb[3 * m + 1] : bb[3 * m + 2];
+                b1own[m] = bb[3 * m];
+            }
+            tvdb_row<R, EX, C, T>(g, vr, bv, dt, seam, F, bn);
+        }
+        const int pk = k & 1, pk1 = (k + 1) & 1;
+        if (live) {
+            float* w = (r <= J) ? FA + (size_t)r * n + g.t * C : FB + ((size_t)pk1 * J + bp) * n + g.t * C;
+#pragma unroll
+            for (int m = 0; m < C; m++)
+                w[m] = F[m];
+        }
+        __syncthreads();
+        // ---- combine and store the owned pencils (A-row groups 0..J-1)
+        if (live && r < J) {
+            int jo = j0 + r;
+            const size_t cell0 = ((size_t)(k % nz) * ny + jo) * n + g.t * C;
+            if (b1s != ub) {
+                float b1c[C * 3];
+                ldg_chunk<float, C * 3>(b1s + cell0 * 3, b1c);
+#pragma unroll
+                for (int m = 0; m < C; m++)
+                    b1own[m] = b1c[3 * m];
+            }
+            const float* fa1 = FA + (size_t)(r + 1) * n + g.t * C;
+            const float* fb = FB + ((size_t)pk * J + r) * n + g.t * C;
+            const float* fbp = FB + ((size_t)pk1 * J + r) * n + g.t * C;
+            const float* b3 = B3 + ((size_t)pk * J + r) * n + g.t * C;
+            float out[C * 3];
+#pragma unroll
+            for (int m = 0; m < C; m++) {
+                float x = b1own[m];
+                x = x - F[m];
+                x = x + fa1[m];
+                x = x - fb[m];
+                x = x + fbp[m];
+                out[3 * m] = x;
+                out[3 * m + 1] = bn[m];
+                out[3 * m + 2] = b3[m];
+            }
+            stg_chunk<float, C * 3>(bo + cell0 * 3, out);
+        }
+        // the B rows' advected b(3) of plane k+1, for the next step
+        if (brow) {
+            float* b3w = B3 + ((size_t)pk1 * J + bp) * n + g.t * C;
+#pragma unroll
+            for (int m = 0; m < C; m++)
+                b3w[m] = bn[m];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace mhd

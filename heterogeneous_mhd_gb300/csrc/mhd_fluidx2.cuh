@@ -66,11 +66,21 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
     const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
     using W = wide_t<R, EX>;
 
-    // ---- gather this thread's cells
-    R q[C][5], f[C][3];
-    {
-        R qf[C * 5], bjf[C * 3], bpf[C * 3], bkf[C * 3];
-        lds_chunk<R, C * 5>(su + (size_t)(lp * n + i0) * 5, qf);
+    // ---- gather this thread's cells.  q and the cell-centred field are read
+    // again from shared memory where they are needed later, which keeps them
+    // out of the registers across the exchange phases.
+    const R* uq = su + (size_t)(lp * n + i0) * 5;
+    auto load_q = [&](R (&q)[C][5]) {
+        R qf[C * 5];
+        lds_chunk<R, C * 5>(uq, qf);
+#pragma unroll
+        for (int m = 0; m < C; m++)
+#pragma unroll
+            for (int s = 0; s < 5; s++)
+                q[m][s] = qf[5 * m + s];
+    };
+    auto load_f = [&](R (&f)[C][3]) {  // C/fluidx.c:71-81: b/2 + b(neighbour face)/2
+        R bjf[C * 3], bpf[C * 3], bkf[C * 3];
         const R* bj = sb + (size_t)(lp * n) * 3;
         lds_chunk<R, C * 3>(bj + 3 * i0, bjf);
         lds_chunk<R, C * 3>(sb + (size_t)((lp + 1) * n + i0) * 3, bpf);
@@ -79,16 +89,16 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
         const R b1next = bj[3 * inext];
 #pragma unroll
         for (int m = 0; m < C; m++) {
-#pragma unroll
-            for (int s = 0; s < 5; s++)
-                q[m][s] = qf[5 * m + s];
             const R h0 = R(0.5) * bjf[3 * m];
             const R h0p = R(0.5) * ((m + 1 < C) ? bjf[3 * (m + 1)] : b1next);
-            f[m][0] = h0 + h0p;                                        // C/fluidx.c:71-78
-            f[m][1] = R(0.5) * bjf[3 * m + 1] + bpf[3 * m + 1] / R(2);  // C/fluidx.c:79
-            f[m][2] = R(0.5) * bjf[3 * m + 2] + bkf[3 * m + 2] / R(2);  // C/fluidx.c:80
+            f[m][0] = h0 + h0p;
+            f[m][1] = R(0.5) * bjf[3 * m + 1] + bpf[3 * m + 1] / R(2);
+            f[m][2] = R(0.5) * bjf[3 * m + 2] + bkf[3 * m + 2] / R(2);
         }
-    }
+    };
+    R q[C][5], f[C][3];
+    load_q(q);
+    load_f(f);
 
     // ---- stage 1 (C/tvd1.c:33-49)
     R fr[C][5], gl[C][5];  // fr = c*wr, gl = c*wl (so fl(i) = gl(i+1))
@@ -144,6 +154,7 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
     // ---- stage 2 (C/tvd1.c:51-116)
     {
         R v[C][5], cmax = R(0);
+        load_f(f);
 #pragma unroll
         for (int m = 0; m < C; m++) {
             R ci;
@@ -216,6 +227,7 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
         g.template shift<5>(flux[C - 1], fprev, -1, seam, 1);
         const R mdt = R(W(-1.0) * W(dt));
         R of[C * 5];
+        load_q(q);
 #pragma unroll
         for (int m = 0; m < C; m++)
 #pragma unroll

@@ -38,6 +38,7 @@ struct AdvectArgs {
     double dt_val;
     const void* dt_ptr;
     int* err;
+    int K;                // planes per CTA along k for the marching kernel (nz % K == 0)
 };
 
 struct TransposeArgs {
