@@ -103,6 +103,7 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
                                           C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                           C.c_int]),
         "mhd_host_divb_max": (C.c_double, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "mhd_calcfl_noalloc": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -65,6 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         ("kernels_fast.cu", [nvcc, *NVCC_COMMON, "-Xptxas", "-v"] if verbose else [nvcc, *NVCC_COMMON]),
         ("kernels_exact.cu", [nvcc, *NVCC_COMMON, "--fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
         ("mhd_abi.cu", [nvcc, *NVCC_COMMON]),
+        ("mhd_noalloc.cu", [nvcc, *NVCC_COMMON]),
     ]
     jobs = []
     for src, base in units:

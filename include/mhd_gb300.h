@@ -158,6 +158,20 @@ MHD_API long long mhd_launch_count(mhd_ctx *ctx);
 /* max |div B| of the current state, computed on the device (synchronous). */
 MHD_API int mhd_divb_max(mhd_ctx *ctx, double *out);
 
+/* 1/max_c of calcfl without any device allocation.  No counterpart in the
+ * reference: it is for callers that cannot let a library allocate device
+ * memory (inside a CUDA-graph stream capture, under a host framework that owns
+ * all device memory, or in a loop that must not enter the allocator).  Its
+ * scratch is a fixed file-scope device array (768 KB per device, held until the
+ * process exits).  u, b and inv_cmax are device pointers; the two kernels are
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) and
+ * *inv_cmax is written when the stream reaches them.  Grids of more than
+ * 134,217,728 cells (512^3) return MHD_ERR_UNSUPPORTED.  The first call on a
+ * device looks up the array's address and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+MHD_API int mhd_calcfl_noalloc(const float *u, const float *b, int nx, int ny, int nz, float *inv_cmax,
+                               void *stream);
+
 /* ------------------------------------------------- initial conditions (host) */
 
 /* Orszag-Tang-like vortex: rho = rho0, p = p0,
