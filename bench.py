@@ -185,6 +185,10 @@ def our_arm(args):
     n = args.size
     cells = n ** 3
     u0, b0 = mhd.init_turbulence(n, seed=rank)
+    tuned = {}
+    if not args.no_tune:  # time the launch-shape candidates on this device first
+        from heterogeneous_mhd_gb300 import autotune
+        tuned = {k: v for k, v in autotune.tune(n, steps=2).items() if not k.startswith("_")}
     ctx = mhd.Context(n, n, n)
     ctx.set_state(u0, b0)
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -275,7 +279,7 @@ def our_arm(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"decaying turbulence {n}^3, FP32, CFL 0.7, {args.variant} Strang step",
                    "grid": [n, n, n], "variant": args.variant, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "state 537 MB > L2, no flush"},
+                   "l2": "state 537 MB > L2, no flush", "launch_shapes": tuned or "planner defaults"},
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": 32 * cells,
                 "d2h_bytes_per_step": 32 * cells, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -306,6 +310,7 @@ def main():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--variant", default="plain", choices=["plain", "fused"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

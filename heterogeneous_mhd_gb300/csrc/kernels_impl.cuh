@@ -61,9 +61,12 @@ static FxPlan plan_fluidx(int nx, int ny, bool aligned)
         else if (nx % 3 == 0 && nx % 4 == 0 && pow2_in(nx / 3, 16, 128))
             p.C = 3, p.T = nx / 3;
         if (p.C) {
+            int target = tune_value(TUNE_FLUIDX_THREADS);
+            if (target != 64 && target != 128 && target != 256)
+                target = 64;  // measured best on GB300 at 256^3 (autotune.py)
             p.P = 0;
             for (int P = 1; P <= ny; P++)
-                if (ny % P == 0 && P * p.T <= 128 && (P * p.T) % 32 == 0)
+                if (ny % P == 0 && P * p.T <= (target > p.T ? target : p.T) && (P * p.T) % 32 == 0 && P * p.T <= 256)
                     p.P = P;
             if (p.P)
                 return p;
@@ -148,36 +151,74 @@ static FxPlan plan_advect(int nx, int ny, bool aligned)
     return p;
 }
 
-// Marching kernel (C = 8, FP32): J pencils per CTA such that the slabs fit
-// two CTAs per SM, K planes per CTA such that there are >= 4 waves.
-static bool plan_advect3(int nx, int ny, int nz, bool aligned, int& T, int& J, int& K)
+// Marching kernel (FP32): C cells per thread (4 by default, or 8), a ring of
+// NS plane slabs (3 by default, or 2), J pencils per CTA (the largest that
+// keeps `ctas` CTAs per SM in shared memory) and K planes per CTA (the
+// largest that still gives >= 4 waves).  Every choice can be overridden by
+// the tuning knobs (advect.cells / slots / J / K).
+struct A3Plan {
+    int C, T, NS, J, K;
+};
+
+static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p)
 {
-    if (!kV2 || !aligned || nx % 8 != 0 || !pow2_in(nx / 8, 4, 64))
+    if (!kV2 || !aligned)
         return false;
-    T = nx / 8;
-    J = 0;
-    for (int j = 1; j <= ny && j <= 16; j++)
-        if (ny % j == 0 && advect3_threads(j, T) <= 384 && advect3_smem_floats(j, T) * 4 <= 113 * 1024)
-            J = j;
-    if (!J)
+    p.C = tune_value(TUNE_ADVECT_C) == 8 ? 8 : 4;
+    p.NS = tune_value(TUNE_ADVECT_SLOTS) == 2 ? 2 : 3;  // three slots measured best (autotune.py)
+    if (nx % p.C != 0)
         return false;
-    K = 1;
-    for (int k = 1; k <= nz && k <= 32; k++)
-        if (nz % k == 0 && (long long)(ny / J) * (nz / k) >= 4 * 2 * 152)
-            K = k;
+    p.T = nx / p.C;
+    if (!(p.C == 4 ? pow2_in(p.T, 8, 128) : pow2_in(p.T, 4, 64)))
+        return false;
+    const int ctas = (p.NS == 2) ? 3 : 2;
+    const size_t smem_cap = (size_t)(224 * 1024) / ctas;
+    const int jt = tune_value(TUNE_ADVECT_J);
+    p.J = 0;
+    for (int j = 1; j <= ny && j <= 16; j++) {
+        const bool fits = advect3_threads(j, p.T) <= 384 && advect3_smem_floats(j, nx, p.NS) * sizeof(float) <= 227 * 1024;
+        if (ny % j != 0 || !fits)
+            continue;
+        if (jt ? (j == jt) : (advect3_smem_floats(j, nx, p.NS) * sizeof(float) <= smem_cap))
+            p.J = j;
+    }
+    if (!p.J)
+        return false;
+    const int kt = tune_value(TUNE_ADVECT_K);
+    p.K = 1;
+    for (int k = 1; k <= nz && k <= 64; k++) {
+        if (nz % k != 0)
+            continue;
+        if (kt ? (k == kt) : ((long long)(ny / p.J) * (nz / k) >= 4LL * ctas * 152 && k <= 32))
+            p.K = k;
+    }
     return true;
 }
 
-template <int T>
+template <int C, int T, int NS>
 static cudaError_t launch_ad3(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    cudaError_t e = allow_smem(k_advect3<EX, T>, attr, true);
+    cudaError_t e = allow_smem(k_advect3<EX, C, T, NS>, attr, true);
     if (e != cudaSuccess)
         return e;
     dim3 grid(a.ny / a.P, a.nz / a.K);
-    k_advect3<EX, T><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, T) * sizeof(float), s>>>(a);
+    k_advect3<EX, C, T, NS><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, a.nx, NS) * sizeof(float), s>>>(a);
     return cudaGetLastError();
+}
+
+template <int C, int NS>
+static cudaError_t launch_ad3_t(const AdvectArgs& a, int T, cudaStream_t s)
+{
+    switch (T) {
+    case 4: if constexpr (C == 8) return launch_ad3<C, 4, NS>(a, s); break;
+    case 8: return launch_ad3<C, 8, NS>(a, s);
+    case 16: return launch_ad3<C, 16, NS>(a, s);
+    case 32: return launch_ad3<C, 32, NS>(a, s);
+    case 64: return launch_ad3<C, 64, NS>(a, s);
+    case 128: if constexpr (C == 4) return launch_ad3<C, 128, NS>(a, s); break;
+    }
+    return cudaErrorInvalidValue;
 }
 
 template <int C, int T>
@@ -198,17 +239,13 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
     const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
                          reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
     if constexpr (kV2) {
-        int T3, J3, K3;
-        if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, T3, J3, K3)) {
-            a.P = J3;
-            a.K = K3;
-            switch (T3) {
-            case 4: return launch_ad3<4>(a, s);
-            case 8: return launch_ad3<8>(a, s);
-            case 16: return launch_ad3<16>(a, s);
-            case 32: return launch_ad3<32>(a, s);
-            case 64: return launch_ad3<64>(a, s);
-            }
+        A3Plan p3;
+        if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3)) {
+            a.P = p3.J;
+            a.K = p3.K;
+            if (p3.C == 4)
+                return (p3.NS == 2) ? launch_ad3_t<4, 2>(a, p3.T, s) : launch_ad3_t<4, 3>(a, p3.T, s);
+            return (p3.NS == 2) ? launch_ad3_t<8, 2>(a, p3.T, s) : launch_ad3_t<8, 3>(a, p3.T, s);
         }
     }
     const FxPlan p = plan_advect(a.nx, a.ny, (al & 15) == 0);

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -116,6 +117,7 @@ struct mhd_ctx {
     int use_graphs = 1;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     double gcfl[2] = {0, 0};
+    long long gtune[2] = {-1, -1};  // tuning generation each graph was captured with
     int glaunches[2] = {0, 0};
     bool capturing = false;
     // profiling
@@ -672,7 +674,7 @@ static int step_graph(mhd_ctx* c, double cfl, int variant)
     const int steady = (int)fluidx_parts(c);
     if (c->cfl_nparts != steady)  // first step after a standalone calcfl
         return step_once_direct(c, cfl, variant);
-    if (!c->gexec[variant] || c->gcfl[variant] != cfl) {
+    if (!c->gexec[variant] || c->gcfl[variant] != cfl || c->gtune[variant] != tune_generation()) {
         if (c->gexec[variant]) {
             cudaGraphExecDestroy(c->gexec[variant]);
             c->gexec[variant] = nullptr;
@@ -698,6 +700,7 @@ static int step_graph(mhd_ctx* c, double cfl, int variant)
         cudaGraphDestroy(g);
         CUDA_TRY(e);
         c->gcfl[variant] = cfl;
+        c->gtune[variant] = tune_generation();
     }
     CUDA_TRY(cudaGraphLaunch(c->gexec[variant], c->stream));
     c->launch_count += c->glaunches[variant];
@@ -783,6 +786,41 @@ extern "C" MHD_API int mhd_profile_reset(mhd_ctx* c)
 }
 
 extern "C" MHD_API long long mhd_launch_count(mhd_ctx* c) { return c ? c->launch_count : -1; }
+
+// ------------------------------------------------------------------ tuning
+
+static std::atomic<int> g_tune[TUNE_COUNT];
+static std::atomic<long long> g_tune_gen{0};
+
+int mhd::tune_value(int key) { return (key >= 0 && key < TUNE_COUNT) ? g_tune[key].load() : 0; }
+long long mhd::tune_generation() { return g_tune_gen.load(); }
+
+static int tune_key(const char* key)
+{
+    static const char* names[TUNE_COUNT] = {"fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K"};
+    if (!key)
+        return -1;
+    for (int k = 0; k < TUNE_COUNT; k++)
+        if (strcmp(key, names[k]) == 0)
+            return k;
+    return -1;
+}
+
+extern "C" MHD_API int mhd_tune_set(const char* key, int value)
+{
+    const int k = tune_key(key);
+    if (k < 0 || value < 0)
+        return set_err(MHD_ERR_ARG);
+    g_tune[k].store(value);
+    g_tune_gen.fetch_add(1);
+    return set_err(MHD_OK);
+}
+
+extern "C" MHD_API int mhd_tune_get(const char* key)
+{
+    const int k = tune_key(key);
+    return (k < 0) ? -1 : g_tune[k].load();
+}
 
 extern "C" MHD_API int mhd_divb_max(mhd_ctx* c, double* out)
 {

@@ -2,12 +2,11 @@
 // tvdb, C/advectbyzxA1.c:18-63 ... C/tvdb.c:10-91).
 //
 // A CTA owns J consecutive pencils (j0..j0+J-1) and K consecutive planes
-// (k0..k0+K-1).  Marching k, it keeps a three-slot ring of plane slabs in
-// shared memory: u pencils j0-1..j0+J and b pencils j0..j0+J of one plane,
-// one bulk TMA copy per pencil (fewer, larger copies measured faster than
-// padded per-group copies that avoid the two-way bank conflicts of the
-// 40-word thread chunks).  The slab of plane k+2 is requested at the start of
-// step k, a whole step ahead of its use.  At step k the CTA computes
+// (k0..k0+K-1).  Marching k, it keeps a ring of NS plane slabs in shared
+// memory: u pencils j0-1..j0+J and b pencils j0..j0+J of one plane, one bulk
+// TMA copy per pencil.  With three slots the slab of plane k+2 is requested
+// at the start of step k; with two it is requested as soon as step k has read
+// plane k.  At step k the CTA computes
 //   * J+1 A rows at plane k   (b(2) advected with the face velocity of j-1, j),
 //   * J   B rows at plane k+1 (b(3) advected with the face velocity of k, k+1),
 // one row per thread group of T = n/C threads, and combines for each owned
@@ -15,16 +14,12 @@
 //   b1_out = (((b1 - FA(j,k)) + FA(j+1,k)) - FB(j,k)) + FB(j,k+1)
 // with FB(.,k) and the advected b(3) of plane k kept from the previous step.
 // Every input pencil is read from global memory once per CTA and every B row
-// is computed once (one extra plane of B rows per K planes).
+// is computed once (one extra plane of B rows per K planes).  With C = 4 the
+// 20-word thread chunks are read without bank conflicts.
 #pragma once
 #include "mhd_advect2.cuh"
 
 namespace mhd {
-
-constexpr int kA3C = 8;             // cells per thread
-constexpr int kA3UW = kA3C * 5;     // u words per thread chunk
-constexpr int kA3BW = kA3C * 3;     // b words per thread chunk
-constexpr int kA3S = 3;             // ring slots
 
 __host__ __device__ inline int advect3_rows(int J) { return 2 * J + 1; }
 
@@ -34,23 +29,21 @@ __host__ __device__ inline int advect3_threads(int J, int T)
     return ((t + 31) / 32) * 32;
 }
 
-// shared memory in floats: 3 u slabs, 3 b slabs, FA[J+1][n], FB[2][J][n],
+// shared memory in floats: NS u slabs, NS b slabs, FA[J+1][n], FB[2][J][n],
 // B3[2][J][n], seam; plus the mbarriers (in the static part)
-__host__ __device__ inline size_t advect3_smem_floats(int J, int T)
+__host__ __device__ inline size_t advect3_smem_floats(int J, int n, int NS)
 {
-    const size_t uslab = (size_t)(J + 2) * T * kA3UW, bslab = (size_t)(J + 1) * T * kA3BW;
-    const size_t n = (size_t)T * kA3C;
-    return kA3S * uslab + kA3S * bslab + (J + 1) * n + 4 * J * n + 2 * 32 * kSeamVals;
+    const size_t uslab = (size_t)(J + 2) * n * 5, bslab = (size_t)(J + 1) * n * 3;
+    return NS * uslab + NS * bslab + (size_t)(J + 1) * n + (size_t)4 * J * n + 2 * 32 * kSeamVals;
 }
 
-template <bool EX, int T>
+template <bool EX, int C, int T, int NS>
 __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
 {
     using R = float;
-    constexpr int C = kA3C;
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint64_t bar[kA3S];
+    __shared__ uint64_t bar[NS];
     const int J = a.P, K = a.K;
     const int NR = advect3_rows(J);
     const int tid = threadIdx.x;
@@ -63,11 +56,11 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     const int j0 = blockIdx.x * J, k0 = blockIdx.y * K;
     const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
 
-    constexpr int UROW = T * kA3UW, BROW = T * kA3BW;  // words per pencil row
+    constexpr int UROW = n * 5, BROW = n * 3;  // words per pencil row
     const size_t uslab = (size_t)(J + 2) * UROW, bslab = (size_t)(J + 1) * BROW;
-    float* U = reinterpret_cast<float*>(smem_raw);  // [3][J+2][n*5]
-    float* B = U + kA3S * uslab;                      // [3][J+1][n*3]
-    float* FA = B + kA3S * bslab;                     // [J+1][n]
+    float* U = reinterpret_cast<float*>(smem_raw);  // [NS][J+2][n*5]
+    float* B = U + NS * uslab;                        // [NS][J+1][n*3]
+    float* FA = B + NS * bslab;                       // [J+1][n]
     float* FB = FA + (size_t)(J + 1) * n;             // [2][J][n]
     float* B3 = FB + (size_t)2 * J * n;               // [2][J][n]
     float* seam = B3 + (size_t)2 * J * n;
@@ -75,9 +68,8 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
 
-    // ---- slab loads: plane p into ring slot s (one mbarrier per slot).
-    // Issued by warp 0: lane 0 registers the bytes, then one lane per pencil
-    // issues its bulk copy.
+    // ---- slab loads: plane p into ring slot s (one mbarrier per slot),
+    // issued by warp 0: lane 0 registers the bytes, one lane per pencil copies.
     auto load_plane = [&](int p, int s) {
         if (tid < 32) {
             const int pp = ((p % nz) + nz) % nz;
@@ -98,16 +90,16 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
             }
         }
     };
-    // ring slot and mbarrier parity of plane p (slot 0 gets k0-1, k0+2, ...)
-    auto slot_of = [&](int p) { return (p - k0 + 1) % kA3S; };
-    auto parity_of = [&](int p) { return (uint32_t)(((p - k0 + 1) / kA3S) & 1); };
+    // ring slot and mbarrier parity of plane p (slot 0 gets k0-1, k0-1+NS, ...)
+    auto slot_of = [&](int p) { return (p - k0 + 1) % NS; };
+    auto parity_of = [&](int p) { return (uint32_t)(((p - k0 + 1) / NS) & 1); };
 
     // this thread's chunk of u pencil `row` (0 = j0-1) / b pencil `row` (0 = j0) in slot s
     auto u_chunk = [&](int s, int row, float (&out)[C * 5]) {
-        lds_chunk<float, C * 5>(U + s * uslab + (size_t)row * UROW + g.t * kA3UW, out);
+        lds_chunk<float, C * 5>(U + s * uslab + (size_t)row * UROW + g.t * C * 5, out);
     };
     auto b_chunk = [&](int s, int row, float (&out)[C * 3]) {
-        lds_chunk<float, C * 3>(B + s * bslab + (size_t)row * BROW + g.t * kA3BW, out);
+        lds_chunk<float, C * 3>(B + s * bslab + (size_t)row * BROW + g.t * C * 3, out);
     };
     // raw face velocity between two u chunks (C/advectbyzxA1.c:34, C/advectbyzxB1.c:34)
     auto face_v = [&](const float (&um)[C * 5], const float (&uc)[C * 5], float (&vr)[C]) {
@@ -122,17 +114,18 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     };
 
     if (tid == 0)
-        for (int s = 0; s < kA3S; s++)
+        for (int s = 0; s < NS; s++)
             mbar_init(&bar[s], 1);
     __syncthreads();
     load_plane(k0 - 1, slot_of(k0 - 1));
     load_plane(k0, slot_of(k0));
-    load_plane(k0 + 1, slot_of(k0 + 1));
+    if (NS >= 3)
+        load_plane(k0 + 1, slot_of(k0 + 1));
     mbar_wait_bounded(&bar[slot_of(k0 - 1)], parity_of(k0 - 1), a.err);
     mbar_wait_bounded(&bar[slot_of(k0)], parity_of(k0), a.err);
 
     // ---- prologue: B rows of plane k0 (FB and advected b(3) of the first step)
-    const bool brow = live && r > J;   // B-row groups: pencil j0 + (r-J-1)
+    const bool brow = live && r > J;  // B-row groups: pencil j0 + (r-J-1)
     const int bp = r - J - 1;
     {
         const int sm = slot_of(k0 - 1), sc = slot_of(k0);
@@ -158,13 +151,16 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         }
     }
     __syncthreads();
+    if (NS == 2) {  // plane k0-1 is no longer needed
+        fence_proxy_async_smem();
+        load_plane(k0 + 1, slot_of(k0 + 1));
+    }
 
     const float* b1s = static_cast<const float*>(a.b1_src);
     float* bo = static_cast<float*>(a.b_out);
     for (int k = k0; k < k0 + K; k++) {
         const int sk = slot_of(k), sk1 = slot_of(k + 1);
-        // plane k-1's slot is free (the previous step ended with a barrier)
-        if (k + 2 <= k0 + K) {
+        if (NS >= 3 && k + 2 <= k0 + K) {  // plane k-1's slot is free
             fence_proxy_async_smem();
             load_plane(k + 2, slot_of(k + 2));
         }
@@ -198,10 +194,13 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
                 w[m] = F[m];
         }
         __syncthreads();
+        if (NS == 2 && k + 2 <= k0 + K) {  // plane k has been read: refill its slot
+            fence_proxy_async_smem();
+            load_plane(k + 2, sk);
+        }
         // ---- combine and store the owned pencils (A-row groups 0..J-1)
         if (live && r < J) {
-            int jo = j0 + r;
-            const size_t cell0 = ((size_t)(k % nz) * ny + jo) * n + g.t * C;
+            const size_t cell0 = ((size_t)(k % nz) * ny + j0 + r) * n + g.t * C;
             if (b1s != ub) {
                 float b1c[C * 3];
                 ldg_chunk<float, C * 3>(b1s + cell0 * 3, b1c);

@@ -34,4 +34,16 @@ int advect_pencils(int nx, int ny);
 
 cudaError_t launch_copy(const void* src, void* dst, size_t bytes, cudaStream_t s);
 
+// Launch-shape knobs set by mhd_tune_set (0 = the planner's own choice).
+enum TuneKey : int {
+    TUNE_FLUIDX_THREADS = 0,  // threads per CTA of the register-resident fluidx (64/128/256)
+    TUNE_ADVECT_C,            // cells per thread of the marching advectbyzx (4 or 8)
+    TUNE_ADVECT_SLOTS,        // plane-slab ring depth (2 or 3)
+    TUNE_ADVECT_J,            // pencils per CTA along j
+    TUNE_ADVECT_K,            // planes per CTA along k
+    TUNE_COUNT
+};
+int tune_value(int key);
+long long tune_generation();  // bumped by every change (captured graphs are rebuilt)
+
 }  // namespace mhd

@@ -155,6 +155,17 @@ MHD_API int mhd_profile_reset(mhd_ctx *ctx);
 /* Kernel launches made since the context was created (all kernels). */
 MHD_API long long mhd_launch_count(mhd_ctx *ctx);
 
+/* Launch-shape knobs consulted by the kernel planners, for the autotuner
+ * (heterogeneous_mhd_gb300/autotune.py).  Keys: "fluidx.threads" (threads
+ * per CTA of the register-resident fluidx: 64, 128 or 256), "advect.cells"
+ * (cells per thread of the marching advectbyzx: 4 or 8), "advect.slots"
+ * (plane-slab ring depth: 2 or 3), "advect.J" (pencils per CTA), "advect.K"
+ * (planes per CTA).  0 restores the planner's own choice; a value that does
+ * not fit the grid is ignored.  Captured step graphs are rebuilt on the next
+ * mhd_step.  mhd_tune_get returns the current value (-1 for an unknown key). */
+MHD_API int mhd_tune_set(const char *key, int value);
+MHD_API int mhd_tune_get(const char *key);
+
 /* max |div B| of the current state, computed on the device (synchronous). */
 MHD_API int mhd_divb_max(mhd_ctx *ctx, double *out);
 
