@@ -104,6 +104,16 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
                                           C.c_int]),
         "mhd_host_divb_max": (C.c_double, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
         "mhd_calcfl_noalloc": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
+        "mhd_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, _ip, C.c_int]),
+        "mhd_batch_destroy": (C.c_int, [_vp]),
+        "mhd_batch_set_box": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int]),
+        "mhd_batch_get_box": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int]),
+        "mhd_batch_step": (C.c_int, [_vp, C.c_int, C.c_double]),
+        "mhd_batch_sync": (C.c_int, [_vp]),
+        "mhd_batch_time": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "mhd_batch_stream": (_vp, [_vp]),
+        "mhd_batch_launch_count": (C.c_longlong, [_vp]),
+        "mhd_batch_classes": (C.c_int, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -352,3 +362,105 @@ def init_turbulence(n, seed=0, rho0=1.0, p0=1.0, mach=0.5, bx0=0.3, dbrms=0.1, k
 
 def host_divb_max(b, nx, ny, nz) -> float:
     return float(lib().mhd_host_divb_max(_ptr(b), nx, ny, nz, int(b.dtype == np.float64)))
+
+
+# ------------------------------------------------------------ batched boxes
+
+BATCH_EDGES = (32, 48, 64, 96, 128)
+
+
+def batch_config(nboxes: int = 256, seed: int = 0, edges=BATCH_EDGES):
+    """The batched workload: per box its edge, IC seed, plasma beta and rms Mach.
+
+    Edges are uniform over `edges`, beta log-uniform in [0.1, 10], rms Mach
+    uniform in [0.2, 1.0]; each box is a vortex box (init_vortex) with its own
+    seed (seed * 100003 + box), drawn from numpy's PCG64 so the table is the
+    same on every machine.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = rng.choice(np.asarray(edges), size=nboxes)
+    beta = 10.0 ** rng.uniform(-1.0, 1.0, size=nboxes)
+    mach = rng.uniform(0.2, 1.0, size=nboxes)
+    return [dict(n=int(n[i]), seed=int(seed) * 100003 + i, beta=float(beta[i]), mach=float(mach[i]))
+            for i in range(nboxes)]
+
+
+def init_batch_box(box: dict, fp64: bool = False, gamma: float = 5.0 / 3.0):
+    """Initial state of one batched box: the vortex field with p set by beta and v by Mach.
+
+    B = (-sin 2pi y, sin 4pi x, 0)/sqrt(4pi) has <B^2> = 1/(4pi), so
+    beta = 2p/<B^2> gives p = beta/(8pi); with rho = 1 the sound speed is
+    sqrt(gamma p) and <v^2> = 1.005 vscale^2 of the vortex velocity.
+    """
+    p0 = box["beta"] / (8.0 * np.pi)
+    vscale = box["mach"] * np.sqrt(gamma * p0) / np.sqrt(1.005)
+    n = box["n"]
+    return init_vortex(n, n, n, seed=box["seed"], rho0=1.0, p0=p0, vscale=vscale, noise=1e-3 * vscale,
+                       bscale=1.0, fp64=fp64)
+
+
+class Batch:
+    """Many independent periodic cubes stepped together (mhd_batch_* of the C ABI)."""
+
+    def __init__(self, sizes, fp64: bool = False, exact: bool = False):
+        self.sizes = [int(s) for s in sizes]
+        self.fp64 = fp64
+        self.dtype = np.float64 if fp64 else np.float32
+        flags = (MHD_F64 if fp64 else MHD_F32) | (MHD_MODE_EXACT if exact else MHD_MODE_FAST)
+        arr = (C.c_int * len(self.sizes))(*self.sizes)
+        h = C.c_void_p()
+        _check(lib().mhd_batch_create(C.byref(h), len(self.sizes), arr, flags), "mhd_batch_create")
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            lib().mhd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_box(self, box: int, u, b) -> None:
+        if isinstance(u, np.ndarray):
+            u = np.ascontiguousarray(u, dtype=self.dtype)
+            b = np.ascontiguousarray(b, dtype=self.dtype)
+        _check(lib().mhd_batch_set_box(self._h, box, _ptr(u), _ptr(b), Context._where(u)), "mhd_batch_set_box")
+
+    def get_box(self, box: int):
+        n = self.sizes[box] ** 3
+        u = np.empty(5 * n, dtype=self.dtype)
+        b = np.empty(3 * n, dtype=self.dtype)
+        _check(lib().mhd_batch_get_box(self._h, box, _ptr(u), _ptr(b), MHD_HOST), "mhd_batch_get_box")
+        return u, b
+
+    def get_box_into(self, box: int, u, b) -> None:
+        _check(lib().mhd_batch_get_box(self._h, box, _ptr(u), _ptr(b), Context._where(u)), "mhd_batch_get_box")
+
+    def step(self, nsteps: int = 1, cfl: float = 0.7) -> None:
+        _check(lib().mhd_batch_step(self._h, nsteps, cfl), "mhd_batch_step")
+
+    def sync(self) -> None:
+        _check(lib().mhd_batch_sync(self._h), "mhd_batch_sync")
+
+    def time(self, box: int):
+        t, dt = C.c_double(), C.c_double()
+        _check(lib().mhd_batch_time(self._h, box, C.byref(t), C.byref(dt)), "mhd_batch_time")
+        return t.value, dt.value
+
+    def stream(self) -> int:
+        return lib().mhd_batch_stream(self._h) or 0
+
+    def launch_count(self) -> int:
+        return int(lib().mhd_batch_launch_count(self._h))
+
+    def classes(self) -> int:
+        return int(lib().mhd_batch_classes(self._h))

@@ -4,9 +4,11 @@ nvcc compiles the kernel sets for sm_103a only:
   * kernels_fast.cu  - FP32 with FMA contraction (production path);
   * kernels_exact.cu - FP32/FP64 with --fmad=false, bit-identical to the
     reference's C arithmetic;
-  * mhd_abi.cu       - host code of the C ABI;
+  * mhd_abi.cu       - host code of the C ABI (single box);
+  * mhd_batch.cu     - host code of the batched-box API;
+  * mhd_noalloc.cu   - the allocation-free calcfl;
 and gcc compiles the seeded initial conditions (mhd_init.c) with
--ffp-contract=off so they are identical on x86-64 and aarch64.  The four
+-ffp-contract=off so they are identical on x86-64 and aarch64.  The
 translation units build in parallel; the result is
 heterogeneous_mhd_gb300/lib/libmhd_gb300.so.
 """
@@ -66,6 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         ("kernels_exact.cu", [nvcc, *NVCC_COMMON, "--fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
         ("mhd_abi.cu", [nvcc, *NVCC_COMMON]),
         ("mhd_noalloc.cu", [nvcc, *NVCC_COMMON]),
+        ("mhd_batch.cu", [nvcc, *NVCC_COMMON]),
     ]
     jobs = []
     for src, base in units:

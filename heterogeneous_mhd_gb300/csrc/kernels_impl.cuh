@@ -84,7 +84,7 @@ static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
     cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T>, attr, true);
     if (e != cudaSuccess)
         return e;
-    dim3 grid(a.ny / a.P, a.nz);
+    dim3 grid(a.ny / a.P, a.nz, a.bs.count);
     k_fluidx2<R, EX, C, T><<<grid, a.P * T, fluidx2_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
     return cudaGetLastError();
 }
@@ -116,7 +116,7 @@ static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
     cudaError_t e = allow_smem(k_fluidx<R, EX>, attr);
     if (e != cudaSuccess)
         return e;
-    dim3 grid(a.ny / a.P, a.nz);
+    dim3 grid(a.ny / a.P, a.nz, a.bs.count);
     k_fluidx<R, EX><<<grid, fluidx_threads(a.nx, a.P), fluidx_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
     return cudaGetLastError();
 }
@@ -202,7 +202,7 @@ static cudaError_t launch_ad3(const AdvectArgs& a, cudaStream_t s)
     cudaError_t e = allow_smem(k_advect3<EX, C, T, NS>, attr, true);
     if (e != cudaSuccess)
         return e;
-    dim3 grid(a.ny / a.P, a.nz / a.K);
+    dim3 grid(a.ny / a.P, a.nz / a.K, a.bs.count);
     k_advect3<EX, C, T, NS><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, a.nx, NS) * sizeof(float), s>>>(a);
     return cudaGetLastError();
 }
@@ -228,7 +228,7 @@ static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
     cudaError_t e = allow_smem(k_advect2<R, EX, C, T>, attr);
     if (e != cudaSuccess)
         return e;
-    dim3 grid(a.ny / a.P, a.nz);
+    dim3 grid(a.ny / a.P, a.nz, a.bs.count);
     k_advect2<R, EX, C, T><<<grid, advect2_threads(a.P, T), advect2_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
     return cudaGetLastError();
 }
@@ -277,7 +277,7 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
         threads = 512;
     if (threads < 128)
         threads = 128;
-    dim3 grid(a.ny / a.P, a.nz);
+    dim3 grid(a.ny / a.P, a.nz, a.bs.count);
     k_advect<R, EX><<<grid, threads, advect_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
     return cudaGetLastError();
 }
@@ -292,7 +292,7 @@ static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
         const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.b_out) |
                              reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
         if (a.nx % kT3 == 0 && na % kT3 == 0 && (al & 15) == 0) {  // bulk-TMA tiles
-            dim3 grid(a.nx / kT3, na / kT3, nb);
+            dim3 grid(a.nx / kT3, na / kT3, nb * a.bs.count);
             if (a.axis == 1)
                 k_transpose3<1><<<grid, 256, 0, s>>>(a);
             else
@@ -300,7 +300,7 @@ static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
             return cudaGetLastError();
         }
         if (a.nx % kT2 == 0 && na % kT2 == 0 && (al & 3) == 0) {
-            dim3 grid(a.nx / kT2, na / kT2, nb);
+            dim3 grid(a.nx / kT2, na / kT2, nb * a.bs.count);
             if (a.axis == 1)
                 k_transpose2<1><<<grid, 256, 0, s>>>(a);
             else
@@ -309,25 +309,26 @@ static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
         }
     }
     constexpr int T = TTile<R>::E;
-    dim3 grid((a.nx + T - 1) / T, (na + T - 1) / T, nb);
+    dim3 grid((a.nx + T - 1) / T, (na + T - 1) / T, nb * a.bs.count);
     k_transpose<R><<<grid, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ calcfl
 
-static cudaError_t calcfl(const void* u, const void* b, size_t ncell, void* part, int* nparts, cudaStream_t s)
+static cudaError_t calcfl(const void* u, const void* b, size_t ncell, void* part, int* nparts, const BoxStrides& bs,
+                          cudaStream_t s)
 {
     const int blocks = (int)((ncell + 255) / 256);
     *nparts = blocks;
-    k_calcfl<R, EX><<<blocks, 256, 0, s>>>(static_cast<const R*>(u), static_cast<const R*>(b), ncell,
-                                           static_cast<CflPart<R>*>(part));
+    k_calcfl<R, EX><<<dim3(blocks, bs.count), 256, 0, s>>>(static_cast<const R*>(u), static_cast<const R*>(b), ncell,
+                                                           static_cast<CflPart<R>*>(part), bs);
     return cudaGetLastError();
 }
 
 static cudaError_t cfl_finalize(const CflFinalizeArgs& a, cudaStream_t s)
 {
-    k_cfl_finalize<R, EX><<<1, 1024, 0, s>>>(a);
+    k_cfl_finalize<R, EX><<<a.bs.count, 1024, 0, s>>>(a);
     return cudaGetLastError();
 }
 

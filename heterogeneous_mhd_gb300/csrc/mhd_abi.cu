@@ -378,7 +378,7 @@ static int op_calcfl_partials(mhd_ctx* c, const void* u, const void* b, size_t c
 {
     MHD_TRY(c->part.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
     KTimer kt(c, MHD_K_CALCFL);
-    CUDA_TRY(c->ks->calcfl(u, b, cells, c->part.p, np, c->stream));
+    CUDA_TRY(c->ks->calcfl(u, b, cells, c->part.p, np, BoxStrides{}, c->stream));
     return MHD_OK;
 }
 

@@ -183,6 +183,7 @@ __host__ __device__ inline size_t advect2_smem_elems(int n, int P)
 template <typename R, bool EX, int C, int T>
 __global__ void __launch_bounds__(512) k_advect2(AdvectArgs a)
 {
+    select_box(a, blockIdx.z);
     using W = wide_t<R, EX>;
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];

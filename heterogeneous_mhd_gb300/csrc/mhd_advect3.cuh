@@ -40,6 +40,7 @@ __host__ __device__ inline size_t advect3_smem_floats(int J, int n, int NS)
 template <bool EX, int C, int T, int NS>
 __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
 {
+    select_box(a, blockIdx.z);
     using R = float;
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -26,6 +26,7 @@ __host__ __device__ inline size_t fluidx2_smem_elems(int n, int P)
 template <typename R, bool EX, int C, int T>
 __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
 {
+    select_box(a, blockIdx.z, sizeof(CflPart<R>));
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int P = a.P;

@@ -15,6 +15,23 @@ namespace mhd {
 
 // ------------------------------------------------------------------ params
 
+// Batched launches: the boxes of one size class lie at a fixed byte stride
+// from each other in every array, and the box index is blockIdx.z (for the
+// transposes blockIdx.z / their own z extent).  Zero strides = one box.
+struct BoxStrides {
+    size_t u = 0;   // bytes between the u arrays of consecutive boxes
+    size_t b = 0;   // bytes between the b arrays
+    size_t dt = 0;  // bytes between the device clocks (dt) of consecutive boxes
+    int count = 1;  // boxes in the launch (the launchers' grid z extent)
+};
+
+template <typename P>
+__device__ __forceinline__ P* box_ptr(P* p, size_t stride, int box)
+{
+    using C = typename std::conditional<std::is_const<P>::value, const char, char>::type;
+    return p ? reinterpret_cast<P*>(reinterpret_cast<C*>(p) + stride * (size_t)box) : p;
+}
+
 struct FluidxArgs {
     void* u_out;          // u <- sweep(update_u)
     const void* uu;       // update_u
@@ -26,6 +43,7 @@ struct FluidxArgs {
     const void* dt_ptr;   // device dt (type R) written by the CFL finalize kernel
     void* cfl_part;       // optional fused calcfl epilogue: per-CTA partials (CflPart<R>)
     int* err;
+    BoxStrides bs;
 };
 
 struct AdvectArgs {
@@ -39,6 +57,7 @@ struct AdvectArgs {
     const void* dt_ptr;
     int* err;
     int K;                // planes per CTA along k for the marching kernel (nz % K == 0)
+    BoxStrides bs;
 };
 
 struct TransposeArgs {
@@ -48,7 +67,36 @@ struct TransposeArgs {
     const void* ub;
     int nx, ny, nz;
     int axis;             // 1: x<->y (transpose12), 2: x<->z (transpose13, nx == nz)
+    BoxStrides bs;
 };
+
+// Offset every array of a launch to box `box` (the per-CTA partials of the
+// CFL epilogue too: `parts` per box).
+__device__ __forceinline__ void select_box(FluidxArgs& a, int box, size_t part_bytes)
+{
+    a.u_out = box_ptr(a.u_out, a.bs.u, box);
+    a.uu = box_ptr(a.uu, a.bs.u, box);
+    a.ub = box_ptr(a.ub, a.bs.b, box);
+    a.dt_ptr = box_ptr(a.dt_ptr, a.bs.dt, box);
+    a.cfl_part = box_ptr(a.cfl_part, part_bytes * gridDim.x * gridDim.y, box);
+}
+
+__device__ __forceinline__ void select_box(AdvectArgs& a, int box)
+{
+    a.b_out = box_ptr(a.b_out, a.bs.b, box);
+    a.b1_src = box_ptr(a.b1_src, a.bs.b, box);
+    a.uu = box_ptr(a.uu, a.bs.u, box);
+    a.ub = box_ptr(a.ub, a.bs.b, box);
+    a.dt_ptr = box_ptr(a.dt_ptr, a.bs.dt, box);
+}
+
+__device__ __forceinline__ void select_box(TransposeArgs& a, int box)
+{
+    a.u_out = box_ptr(a.u_out, a.bs.u, box);
+    a.b_out = box_ptr(a.b_out, a.bs.b, box);
+    a.uu = box_ptr(a.uu, a.bs.u, box);
+    a.ub = box_ptr(a.ub, a.bs.b, box);
+}
 
 template <typename R>
 struct CflPart {          // one per CTA of a CFL reduction
@@ -68,6 +116,7 @@ struct CflFinalizeArgs {
     void* clock;          // R[4]: t, tf, dt, 1/c
     long long* nsteps;    // incremented when advance
     int* err;
+    BoxStrides bs;        // batched: u, b and clock strides; nparts is per box
 };
 
 // ------------------------------------------------------------- reductions
@@ -149,6 +198,7 @@ __host__ __device__ inline size_t fluidx_smem_elems(int n, int P)
 template <typename R, bool EX>
 __global__ void __launch_bounds__(512) k_fluidx(FluidxArgs a)
 {
+    select_box(a, blockIdx.z, sizeof(CflPart<R>));
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = a.nx, P = a.P;
     const int np = n * P;
@@ -368,6 +418,7 @@ __host__ __device__ inline size_t advect_smem_elems(int n, int P)
 template <typename R, bool EX>
 __global__ void __launch_bounds__(512) k_advect(AdvectArgs a)
 {
+    select_box(a, blockIdx.z);
     using W = wide_t<R, EX>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = a.nx, P = a.P;
@@ -547,8 +598,10 @@ __global__ void __launch_bounds__(256) k_transpose(TransposeArgs a)
     __shared__ R su[kTT][kTT * 5 + 1];
     __shared__ R sb[kTT][kTT * 3 + 1];
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int i0 = blockIdx.x * kTT, a0 = blockIdx.y * kTT, z = blockIdx.z;
     const int na = (a.axis == 1) ? ny : nz;  // extent of the swapped axis
+    const int nbz = (a.axis == 1) ? nz : ny;  // extent of the untouched axis
+    const int i0 = blockIdx.x * kTT, a0 = blockIdx.y * kTT, z = blockIdx.z % nbz;
+    select_box(a, blockIdx.z / nbz);
     const int ti = min(kTT, nx - i0), ta = min(kTT, na - a0);
     const R* uu = static_cast<const R*>(a.uu);
     const R* ub = static_cast<const R*>(a.ub);
@@ -605,10 +658,14 @@ static __global__ void __launch_bounds__(256) k_copy4(const float* __restrict__ 
 // index in the range.
 template <typename R, bool EX>
 __global__ void __launch_bounds__(256) k_calcfl(const R* __restrict__ u, const R* __restrict__ b, size_t ncell,
-                                                CflPart<R>* part)
+                                                CflPart<R>* part, BoxStrides bs)
 {
     __shared__ R rm[8];
     __shared__ int rn[8];
+    // batched: box blockIdx.y, its partials after those of the boxes before it
+    u = box_ptr(u, bs.u, blockIdx.y);
+    b = box_ptr(b, bs.b, blockIdx.y);
+    part += (size_t)blockIdx.y * gridDim.x;
     const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     R sp = R(0);
     bool isn = false;
@@ -657,7 +714,14 @@ __global__ void __launch_bounds__(1024) k_cfl_finalize(CflFinalizeArgs a)
     using W = wide_t<R, EX>;
     __shared__ R rm[32];
     __shared__ int rn[32];
-    const CflPart<R>* part = static_cast<const CflPart<R>*>(a.part);
+    // batched: one CTA per box (blockIdx.x), each with its own partials, state and clock
+    const int box = blockIdx.x;
+    a.u = box_ptr(a.u, a.bs.u, box);
+    a.b = box_ptr(a.b, a.bs.b, box);
+    a.clock = box_ptr(a.clock, a.bs.dt, box);
+    if (box != 0)
+        a.nsteps = nullptr;
+    const CflPart<R>* part = static_cast<const CflPart<R>*>(a.part) + (size_t)box * a.nparts;
     R m = R(0);
     int ln = -1;
     for (int s = threadIdx.x; s < a.nparts; s += blockDim.x) {

@@ -16,7 +16,8 @@ struct KernelSet {
     cudaError_t (*advect)(const AdvectArgs&, cudaStream_t);
     cudaError_t (*transpose)(const TransposeArgs&, cudaStream_t);
     // first CFL pass over ncell cells; returns the number of partials written
-    cudaError_t (*calcfl)(const void* u, const void* b, size_t ncell, void* part, int* nparts, cudaStream_t);
+    cudaError_t (*calcfl)(const void* u, const void* b, size_t ncell, void* part, int* nparts, const BoxStrides& bs,
+                          cudaStream_t);
     cudaError_t (*cfl_finalize)(const CflFinalizeArgs&, cudaStream_t);
     cudaError_t (*divb)(const void* b, int nx, int ny, int nz, double* part, int* nparts, cudaStream_t);
     size_t part_bytes; // sizeof(CflPart<R>)

@@ -19,7 +19,9 @@ __global__ void __launch_bounds__(256, 4) k_transpose2(TransposeArgs a)
     __shared__ float su[kT2 * kT2U];
     __shared__ float sb[kT2 * kT2B];
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int i0 = blockIdx.x * kT2, a0 = blockIdx.y * kT2, z = blockIdx.z;
+    const int nbz = (AXIS == 1) ? nz : ny;  // extent of the untouched axis
+    const int i0 = blockIdx.x * kT2, a0 = blockIdx.y * kT2, z = blockIdx.z % nbz;
+    select_box(a, blockIdx.z / nbz);
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
     float* uo = static_cast<float*>(a.u_out);

@@ -23,7 +23,9 @@ __global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
     __shared__ __align__(16) float sb[kT3 * kT3B];
     __shared__ uint64_t bar;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int i0 = blockIdx.x * kT3, a0 = blockIdx.y * kT3, z = blockIdx.z;
+    const int nbz = (AXIS == 1) ? nz : ny;  // extent of the untouched axis
+    const int i0 = blockIdx.x * kT3, a0 = blockIdx.y * kT3, z = blockIdx.z % nbz;
+    select_box(a, blockIdx.z / nbz);
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;

@@ -183,6 +183,28 @@ MHD_API int mhd_divb_max(mhd_ctx *ctx, double *out);
 MHD_API int mhd_calcfl_noalloc(const float *u, const float *b, int nx, int ny, int nz, float *inv_cmax,
                                void *stream);
 
+/* ------------------------------------------------------------ batched boxes */
+
+/* Many independent periodic cubes advanced together, each with its own dt.
+ * No counterpart in the reference, whose driver runs one box per process
+ * (C/mhd.c:18-128); each box takes exactly the steps mhd_step takes on it.
+ * Boxes of equal edge share a size class whose states are contiguous, so each
+ * operator of the step is one launch per class; a whole step of every class is
+ * one CUDA graph.  sizes[i] is the edge of box i (1..512); flags as mhd_create.
+ * Every box must be loaded with mhd_batch_set_box (which also resets its clock
+ * to t = 0) before mhd_batch_step.  Boxes are never clamped to a final time. */
+typedef struct mhd_batch mhd_batch;
+MHD_API int mhd_batch_create(mhd_batch **out, int nboxes, const int *sizes, int flags);
+MHD_API int mhd_batch_destroy(mhd_batch *batch);
+MHD_API int mhd_batch_set_box(mhd_batch *batch, int box, const void *u, const void *b, int where);
+MHD_API int mhd_batch_get_box(mhd_batch *batch, int box, void *u, void *b, int where);
+MHD_API int mhd_batch_step(mhd_batch *batch, int nsteps, double cfl);
+MHD_API int mhd_batch_sync(mhd_batch *batch);  /* also reports device-side errors */
+MHD_API int mhd_batch_time(mhd_batch *batch, int box, double *t, double *dt);
+MHD_API void *mhd_batch_stream(mhd_batch *batch);
+MHD_API long long mhd_batch_launch_count(mhd_batch *batch);
+MHD_API int mhd_batch_classes(mhd_batch *batch);
+
 /* ------------------------------------------------- initial conditions (host) */
 
 /* Orszag-Tang-like vortex: rho = rho0, p = p0,

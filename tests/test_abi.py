@@ -54,6 +54,32 @@ def test_error_strings_and_argument_checks(mhd):
     assert L.mhd_last_error() == 1
     L.calcfl(None, None, None, None, None)
     assert L.mhd_last_error() == 1
+    # batched boxes: edges outside 1..512 and empty batches, before any CUDA call
+    for sizes in ([32, 0], [513], [-4]):
+        arr = (C.c_int * len(sizes))(*sizes)
+        assert L.mhd_batch_create(C.byref(h), len(sizes), arr, 0) == 1
+    assert L.mhd_batch_create(C.byref(h), 0, (C.c_int * 1)(32), 0) == 1
+    assert L.mhd_batch_step(None, 1, 0.7) == 1
+    assert L.mhd_batch_set_box(None, 0, None, None, 0) == 1
+
+
+def test_batch_config_table(mhd):
+    cfg = mhd.batch_config(256, seed=0)
+    assert cfg == mhd.batch_config(256, seed=0)
+    assert {x["n"] for x in cfg} == set(mhd.BATCH_EDGES)
+    assert all(0.1 <= x["beta"] <= 10 and 0.2 <= x["mach"] <= 1.0 for x in cfg)
+    assert len({x["seed"] for x in cfg}) == 256
+    # p and v follow beta and Mach (rho = 1, gamma = 5/3, <B^2> = 1/(4 pi))
+    box = dict(n=16, seed=4, beta=2.0, mach=0.5)
+    u, b = mhd.init_batch_box(box)
+    U, B = u.reshape(-1, 5).astype(np.float64), b.reshape(-1, 3).astype(np.float64)
+    ekin = 0.5 * (U[:, 1:4] ** 2).sum(1) / U[:, 0]
+    B4 = B.reshape(16, 16, 16, 3)  # (k, j, i, component); B_c is the face average
+    bc = 0.5 * (B4 + np.stack([np.roll(B4[..., c], -1, axis=2 - c) for c in range(3)], axis=-1))
+    p = (U[:, 4] - ekin - 0.5 * (bc.reshape(-1, 3) ** 2).sum(1)) * (2.0 / 3.0)
+    assert np.allclose(p, 2.0 / (8 * np.pi), rtol=1e-4)
+    v_rms = np.sqrt(((U[:, 1:4] / U[:, :1]) ** 2).sum(1).mean())
+    assert abs(v_rms / np.sqrt(5.0 / 3.0 * 2.0 / (8 * np.pi)) - 0.5) < 0.02
 
 
 def test_no_cpu_fallback_in_product():

@@ -1,0 +1,116 @@
+"""Batched boxes (mhd_batch_*): many independent cubes of uneven edge, each
+with its own dt, stepped together with one launch per size class per operator.
+
+Each box of a batch must take exactly the steps a single-box context takes on
+it: bit for bit against mhd_step for both arithmetic policies, and bit for bit
+against the oracle (C/mhd.c:59-124 restated) for the EXACT kernels.
+"""
+import numpy as np
+import pytest
+
+from util import bitwise_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def single(mhd, u0, b0, n, nsteps, exact):
+    with mhd.Context(n, n, n, exact=exact) as ctx:
+        ctx.set_state(u0, b0)
+        ctx.step(nsteps, cfl=0.7)
+        u, b = ctx.get_state()
+        t, dt, _ = ctx.time()
+    return u, b, t, dt
+
+
+def make_batch(mhd, boxes, exact):
+    bt = mhd.Batch([x["n"] for x in boxes], exact=exact)
+    ics = []
+    for i, box in enumerate(boxes):
+        u0, b0 = mhd.init_batch_box(box)
+        bt.set_box(i, u0, b0)
+        ics.append((u0, b0))
+    return bt, ics
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_batch_equals_single_box_steps(exact, mhd, cuda):
+    # uneven edges: TMA-aligned classes, a ragged one (17, 30) and repeats
+    cfg = mhd.batch_config(9, seed=3, edges=(16, 17, 30, 32, 48))
+    cfg[0]["n"], cfg[1]["n"] = 17, 30
+    bt, ics = make_batch(mhd, cfg, exact)
+    with bt:
+        bt.step(4)
+        bt.sync()
+        for i, box in enumerate(cfg):
+            u, b = bt.get_box(i)
+            t, dt = bt.time(i)
+            su, sb, st, sdt = single(mhd, *ics[i], box["n"], 4, exact)
+            assert bitwise_equal(u, su) and bitwise_equal(b, sb), (i, box)
+            assert t == st and dt == sdt, (i, t, st)
+
+
+def test_batch_exact_bitwise_vs_oracle(mhd, cuda, oracle32):
+    cfg = mhd.batch_config(40, seed=11)
+    sample = [0, 1, 2, 3, 5, 8]
+    boxes = [cfg[i] for i in sample]
+    # one box of each edge in the sample at most 64^3 keeps the oracle within seconds
+    for x, n in zip(boxes, (32, 48, 64, 32, 48, 32)):
+        x["n"] = n
+    bt, ics = make_batch(mhd, boxes, exact=True)
+    with bt:
+        bt.step(5)
+        bt.sync()
+        for i, box in enumerate(boxes):
+            n = box["n"]
+            u, b = bt.get_box(i)
+            ou, ob, ot, _, _ = oracle32.strang(*ics[i], n, n, n, 5, 0.7)
+            assert bitwise_equal(u, ou) and bitwise_equal(b, ob), (i, box)
+            t, _ = bt.time(i)
+            assert np.float32(t) == np.float32(ot)
+
+
+def test_batch_boxes_keep_own_dt_and_graph_launches(mhd, cuda):
+    cfg = mhd.batch_config(12, seed=5)
+    bt, _ = make_batch(mhd, cfg, exact=False)
+    with bt:
+        ncls = bt.classes()
+        assert ncls == len({x["n"] for x in cfg})
+        bt.step(2)  # first step runs uncaptured (standalone calcfl), the second one is a graph
+        c0 = bt.launch_count()
+        bt.step(3)
+        bt.sync()
+        assert bt.launch_count() - c0 == 3 * 17 * ncls  # 16 operators + the dt finalize per class
+        dts = [bt.time(i)[1] for i in range(len(cfg))]
+        assert all(np.isfinite(dts)) and min(dts) > 0
+        assert len(set(dts)) > 1  # beta and Mach differ per box, so does dt
+
+
+def test_batch_unloaded_box_is_refused(mhd, cuda):
+    with mhd.Batch([32, 32]) as bt:
+        u0, b0 = mhd.init_batch_box(dict(n=32, seed=1, beta=1.0, mach=0.5))
+        bt.set_box(0, u0, b0)
+        with pytest.raises(mhd.MhdError):
+            bt.step(1)
+        bt.set_box(1, u0, b0)
+        bt.step(1)
+        bt.sync()
+        a, _ = bt.get_box(0)
+        c, _ = bt.get_box(1)
+        assert bitwise_equal(a, c)
+
+
+def test_batch_device_buffers(mhd, cuda):
+    torch = cuda
+    box = dict(n=48, seed=2, beta=0.5, mach=0.8)
+    u0, b0 = mhd.init_batch_box(box)
+    du, db = torch.from_numpy(u0).cuda(), torch.from_numpy(b0).cuda()
+    with mhd.Batch([48, 32]) as bt:
+        bt.set_box(0, du, db)
+        bt.set_box(1, *mhd.init_batch_box(dict(n=32, seed=3, beta=2.0, mach=0.3)))
+        bt.step(2)
+        bt.sync()
+        ou, ob = torch.empty_like(du), torch.empty_like(db)
+        bt.get_box_into(0, ou, ob)
+        torch.cuda.synchronize()
+        hu, hb = bt.get_box(0)
+        assert bitwise_equal(ou.cpu().numpy(), hu) and bitwise_equal(ob.cpu().numpy(), hb)
