@@ -78,10 +78,14 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        t0 = time.perf_counter()  # nvidia-smi takes a moment to start: wait for its first sample
+        while time.perf_counter() - t0 < 5.0 and self.path.stat().st_size == 0 and self.proc.poll() is None:
+            time.sleep(0.02)
         return self
 
     def __exit__(self, *exc):
@@ -113,6 +117,19 @@ class ClockSampler:
         self.path.unlink(missing_ok=True)
         return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def measured_traffic(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture
+    (profiles/traffic_256.json) when it was taken on this grid, else None."""
+    p = ROOT / "profiles" / "traffic_256.json"
+    try:
+        t = json.loads(p.read_text())
+    except (OSError, ValueError):
+        return None
+    if t.get("grid") != [n, n, n] or kernel not in t:
+        return None
+    return t[kernel]["dram_bytes_per_launch"]
 
 
 def cpu_baseline(size: int, seconds: float = 12.0):
@@ -169,6 +186,30 @@ def reference_arm(args):
                                        f"pencils, {cores} threads"},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def fp64_error_leg(mhd, n: int, steps: int):
+    """Per-field relative L2 of the FP32 kernels (FAST, the production path,
+    and EXACT) against the FP64 build of the same method, after `steps`
+    steps of the turbulence box from the same initial state."""
+    from heterogeneous_mhd_gb300.diagnostics import field_errors
+
+    out = {"grid": [n, n, n], "steps": steps, "reference": "FP64 build of the same kernels (EXACT policy)"}
+    u64, b64 = mhd.init_turbulence(n, seed=0, fp64=True)
+    u32, b32 = u64.astype(np.float32), b64.astype(np.float32)
+    t0 = time.perf_counter()
+    with mhd.Context(n, n, n, fp64=True, exact=True) as ctx:
+        ctx.set_state(u64, b64)
+        ctx.step(steps, cfl=0.7)
+        ru, rb = ctx.get_state()
+    out["fp64_seconds"] = time.perf_counter() - t0
+    for name, exact in (("fast_f32", False), ("exact_f32", True)):
+        with mhd.Context(n, n, n, exact=exact) as ctx:
+            ctx.set_state(u32, b32)
+            ctx.step(steps, cfl=0.7)
+            fu, fb = ctx.get_state()
+        out[name] = {k: float(f"{v:.3e}") for k, v in field_errors(fu, fb, ru, rb).items()}
+    return out
 
 
 def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3):
@@ -295,6 +336,7 @@ def our_arm(args):
     # roofline of the dominant kernel
     hbm, src = peaks()
     dom = max((k for k in kern if kern[k][1] > 0), key=lambda k: kern[k][0])
+    traffic = measured_traffic(dom, n)
     tot_ms, nl = kern[dom]
     mean_ms = tot_ms / nl
     achieved = ALG_BYTES[dom] * cells / (mean_ms * 1e-3) / 1e9
@@ -315,7 +357,7 @@ def our_arm(args):
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": 32 * cells,
                 "d2h_bytes_per_step": 32 * cells, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": src, "traffic": None,
+                     "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
                      "alg_bytes_per_launch": ALG_BYTES[dom] * cells, "mean_launch_ms": mean_ms,
                      "step_alg_gbs": step_bw, "step_frac": step_bw / hbm},
         "kernels": {k: {"ms_total": round(v[0], 4), "launches": v[1], "share": share.get(k, 0.0)}
@@ -326,6 +368,8 @@ def our_arm(args):
         "status": int(status),
     }
     ctx.close()
+    if not args.no_fp64:
+        line["fp64_error"] = fp64_error_leg(mhd, n, args.fp64_steps)
     if not args.no_batch:
         line["batch"] = batch_leg(mhd, torch, rank)
     if world == 1 and not args.no_cpu:
@@ -333,6 +377,22 @@ def our_arm(args):
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def ncu_case(args):
+    """A short run for ncu captures: `--size`^3 turbulence, planner launch
+    shapes (no autotuner), graphs off so every kernel is a direct launch;
+    one warm-up step and two measured steps, no JSON line."""
+    import heterogeneous_mhd_gb300 as mhd
+
+    n = args.size
+    u0, b0 = mhd.init_turbulence(n, seed=0)
+    with mhd.Context(n, n, n) as ctx:
+        ctx.use_graphs(False)
+        ctx.set_state(u0, b0)
+        ctx.step(3, cfl=0.7, fused=args.variant == "fused")
+        ctx.sync()
+        assert ctx.check() == mhd.MHD_OK
 
 
 def main():
@@ -346,10 +406,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-boxes leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error leg")
+    ap.add_argument("--ncu-case", action="store_true", help="run the short profiling case only")
+    ap.add_argument("--fp64-steps", type=int, default=100, help="steps of the FP64 error leg")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
+    if args.ncu_case:
+        ncu_case(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         our_arm(args)
