@@ -7,6 +7,8 @@ nvcc compiles the kernel sets for sm_103a only:
   * mhd_abi.cu       - host code of the C ABI (single box);
   * mhd_batch.cu     - host code of the batched-box API;
   * mhd_noalloc.cu   - the allocation-free calcfl;
+  * closure.cu       - the learned closure (BF16 tensor-core convolutions,
+    loss, optimiser, filter and correction kernels);
 and gcc compiles the seeded initial conditions (mhd_init.c) with
 -ffp-contract=off so they are identical on x86-64 and aarch64.  The
 translation units build in parallel; the result is
@@ -62,13 +64,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile every translation unit that changed and link the library."""
     nvcc = _nvcc()
     OBJDIR.mkdir(parents=True, exist_ok=True)
-    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "mhd_gb300.h"]
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
     units = [
         ("kernels_fast.cu", [nvcc, *NVCC_COMMON, "-Xptxas", "-v"] if verbose else [nvcc, *NVCC_COMMON]),
         ("kernels_exact.cu", [nvcc, *NVCC_COMMON, "--fmad=false", "-prec-div=true", "-prec-sqrt=true"]),
         ("mhd_abi.cu", [nvcc, *NVCC_COMMON]),
         ("mhd_noalloc.cu", [nvcc, *NVCC_COMMON]),
         ("mhd_batch.cu", [nvcc, *NVCC_COMMON]),
+        ("closure.cu", [nvcc, *NVCC_COMMON]),
     ]
     jobs = []
     for src, base in units:
