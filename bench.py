@@ -212,6 +212,29 @@ def fp64_error_leg(mhd, n: int, steps: int):
     return out
 
 
+CLOSURE_WEIGHTS = ROOT / "heterogeneous_mhd_gb300" / "closure_weights.npz"
+
+
+def closure_leg(seeds=(1000,), fine=256, factor=4, crossings=2.0):
+    """The closure at matched error: a held-out vortex seed run to `crossings`
+    turbulent crossing times at fine^3 (plain) and at (fine/factor)^3 (plain,
+    and plain + the trained closure after every step), compared after
+    filtering the fine run; GPU time of the fine run over the closure run."""
+    if not CLOSURE_WEIGHTS.exists():
+        return {"unavailable": "no trained closure weights in the package"}
+    from heterogeneous_mhd_gb300 import closure, closure_train
+
+    net = closure.ClosureNet.load(CLOSURE_WEIGHTS)
+    rep = closure_train.evaluate(net, list(seeds), fine, factor, crossings, log=None)
+    out = {"workload": f"vortex seeds {list(seeds)}, {fine}^3 plain vs {fine // factor}^3 plain and "
+                       f"{fine // factor}^3 + closure, {crossings} crossing times", **rep["summary"]}
+    r = rep["runs"][0]
+    out.update({"fine_ms": r["fine_ms"], "closure_ms": r["closure"]["wall_ms"], "plain_coarse_ms": r["plain"]["wall_ms"],
+                "closure_divb_max": r["closure"]["divb_max"], "closure_fallbacks": r["closure"]["fallbacks"],
+                "closure_steps": r["closure"]["steps"]})
+    return out
+
+
 def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3):
     """The batched workload: 256 vortex boxes of edge 32..128 with their own
     beta, Mach and dt, FP32, one graph per step; 50 timed steps."""
@@ -372,6 +395,8 @@ def our_arm(args):
         line["fp64_error"] = fp64_error_leg(mhd, n, args.fp64_steps)
     if not args.no_batch:
         line["batch"] = batch_leg(mhd, torch, rank)
+    if not args.no_closure:
+        line["closure"] = closure_leg()
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n)
     print(json.dumps(line), flush=True)
@@ -407,6 +432,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-boxes leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error leg")
+    ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure leg")
     ap.add_argument("--ncu-case", action="store_true", help="run the short profiling case only")
     ap.add_argument("--fp64-steps", type=int, default=100, help="steps of the FP64 error leg")
     args = ap.parse_args()

@@ -197,24 +197,31 @@ class ClosureNet:
 
     # ---- buffers
     def ensure(self, nb: int, n: int) -> None:
+        """Buffers for batches of nb boxes of edge n (kept per shape)."""
         if self._shape == (nb, n):
             return
-        torch = self.torch
-        nv = nb * n ** 3
-        bf = dict(dtype=torch.bfloat16, device=self.dev)
-        self.a = [torch.empty(nv * HIDDEN, **bf) for _ in range(NLAYERS)]
-        self.z = [torch.empty(nv * HIDDEN, **bf) for _ in range(NLAYERS)]
-        self.out = torch.empty(nv * 8, dtype=torch.float32, device=self.dev)
-        self.dout = torch.empty(nv * 16, **bf)
-        self.dz = [torch.empty(nv * HIDDEN, **bf) for _ in range(2)]
-        self.rb = torch.empty(nv * 3, dtype=torch.float32, device=self.dev)
-        self.lsc = torch.empty(512, dtype=torch.float32, device=self.dev)
-        self.loss_dev = torch.zeros(1, dtype=torch.float32, device=self.dev)
-        ws = max(int(cl().mhd_cl_wgrad_scratch(k, nb, n)) for k in (WG_IN, WG_HID, WG_HEAD))
-        if ws < 0:
-            raise MhdError(1, f"box edge {n} is not supported by the closure kernels")
-        self.wsc = torch.empty(ws // 4 + 1, dtype=torch.float32, device=self.dev)
-        self.csc = torch.empty(256 * HIDDEN, dtype=torch.float32, device=self.dev)
+        if not hasattr(self, "_bufs"):
+            self._bufs = {}
+        if (nb, n) not in self._bufs:
+            torch = self.torch
+            nv = nb * n ** 3
+            bf = dict(dtype=torch.bfloat16, device=self.dev)
+            ws = max(int(cl().mhd_cl_wgrad_scratch(k, nb, n)) for k in (WG_IN, WG_HID, WG_HEAD))
+            if ws < 0:
+                raise MhdError(1, f"box edge {n} is not supported by the closure kernels")
+            self._bufs[(nb, n)] = dict(
+                a=[torch.empty(nv * HIDDEN, **bf) for _ in range(NLAYERS)],
+                z=[torch.empty(nv * HIDDEN, **bf) for _ in range(NLAYERS)],
+                out=torch.empty(nv * 8, dtype=torch.float32, device=self.dev),
+                dout=torch.empty(nv * 16, **bf),
+                dz=[torch.empty(nv * HIDDEN, **bf) for _ in range(2)],
+                rb=torch.empty(nv * 3, dtype=torch.float32, device=self.dev),
+                lsc=torch.empty(512, dtype=torch.float32, device=self.dev),
+                loss_dev=torch.zeros(1, dtype=torch.float32, device=self.dev),
+                wsc=torch.empty(ws // 4 + 1, dtype=torch.float32, device=self.dev),
+                csc=torch.empty(256 * HIDDEN, dtype=torch.float32, device=self.dev))
+        for k, v in self._bufs[(nb, n)].items():
+            setattr(self, k, v)
         self._shape = (nb, n)
 
     # ---- forward / backward
@@ -316,14 +323,20 @@ class Corrector:
         self.ut = t.empty(nv * 5, dtype=t.float32, device=net.dev)
         self.bt = t.empty(nv * 3, dtype=t.float32, device=net.dev)
         self.flags = t.zeros(2, dtype=t.int32, device=net.dev)
-        self.esum = t.zeros(2, dtype=t.float64, device=net.dev)
+        self.esum = t.zeros(8, dtype=t.float64, device=net.dev)
         self.fallbacks = t.zeros(1, dtype=t.int64, device=net.dev)
         self.applied = 0
 
-    def predict(self, u_ptr: int, b_ptr: int) -> None:
-        """Net output for the state at (u_ptr, b_ptr) (features of the pre-step state)."""
+    def features(self, u_ptr: int, b_ptr: int) -> None:
+        """Net input from the state at (u_ptr, b_ptr): the only read of the state."""
         self.net.features(u_ptr, b_ptr, self.n, self.x)
+
+    def forward(self) -> None:
         self.net.forward(self.x, 1, self.n)
+
+    def predict(self, u_ptr: int, b_ptr: int) -> None:
+        self.features(u_ptr, b_ptr)
+        self.forward()
 
     def apply(self, u_ptr: int, b_ptr: int) -> None:
         """Correct the state in place with the last prediction (or fall back)."""

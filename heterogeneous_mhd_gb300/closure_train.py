@@ -1,0 +1,367 @@
+"""Training data, training and evaluation of the learned closure.
+
+* generate(): the solver makes its own training pairs.  A fine vortex run
+  (init_vortex, seeded) is sampled every `every` steps; each sample is box
+  filtered to the coarse grid (input), one plain coarse step is taken from
+  it, and a copy of the fine run is advanced to exactly the same physical
+  time (the coarse step's 2 dt, times the refinement factor in fine grid
+  units, as the final time of the fine clock).  The target is the filtered
+  fine state minus the coarse step.
+* train(): AdamW on batches of whole coarse boxes (the convolution is
+  periodic) with a cosine learning-rate decay, all on the GPU kernels.
+* evaluate(): held-out seeds run to a number of turbulent crossing times
+  three ways (fine plain, coarse plain, coarse plain + closure after every
+  step) and compared after filtering the fine run: relative L2 of density,
+  kinetic and magnetic shell spectra, div B, positivity, fallback count and
+  GPU time.
+
+The reference has no learned closure; the solver calls are this package's.
+Run as `python -m heterogeneous_mhd_gb300.closure_train --help`.
+"""
+from __future__ import annotations
+
+import argparse
+import functools
+import json
+import math
+import time
+
+import numpy as np
+
+from . import MHD_DEVICE, Context, _check, init_vortex, lib
+from . import closure as cl
+from .diagnostics import energy_spectra, field_errors, spectrum_error
+
+
+def _torch():
+    return cl._torch()
+
+
+def reached(t: float, tf: float) -> bool:
+    """The clock is at tf: the device clock is FP32 and the tf clamp can leave
+    it an ulp short of tf (t + 2 (tf - t)/2 rounds down), where every further
+    step has dt at round-off."""
+    return t >= tf * (1.0 - 1e-6)
+
+
+def _set_state_dev(ctx: Context, u_ptr: int, b_ptr: int) -> None:
+    _check(lib().mhd_set_state(ctx.handle, u_ptr, b_ptr, MHD_DEVICE), "mhd_set_state")
+
+
+def _get_state_dev(ctx: Context, u, b) -> None:
+    _check(lib().mhd_get_state(ctx.handle, u.data_ptr(), b.data_ptr(), MHD_DEVICE), "mhd_get_state")
+
+
+def v_rms(u) -> float:
+    U = np.asarray(u, dtype=np.float64).reshape(-1, 5)
+    return float(np.sqrt(((U[:, 1:4] / U[:, :1]) ** 2).sum(1).mean()))
+
+
+class Dataset:
+    """Raw FP32 features and targets on the device, then normalised BF16 copies."""
+
+    def __init__(self, nsamples: int, n: int):
+        torch = _torch()
+        self.n, self.count = n, 0
+        nv = n ** 3
+        self.raw_x = torch.empty((nsamples, nv * 8), dtype=torch.float32, device="cuda")
+        self.raw_t = torch.empty((nsamples, nv * 8), dtype=torch.float32, device="cuda")
+        self.x = self.t = None
+        self.stats = None
+
+    def finalize(self) -> cl.Stats:
+        """Channel statistics, then BF16 inputs [S][n^3][16] and targets [S][n^3][8]."""
+        torch = _torch()
+        S, nv = self.count, self.n ** 3
+        s = cl.stream_ptr()
+        sums = torch.zeros(16, dtype=torch.float64, device="cuda")
+        tsum = torch.zeros(16, dtype=torch.float64, device="cuda")
+        _check(cl.cl().mhd_cl_moments(self.raw_x.data_ptr(), 8, S * nv, sums.data_ptr(), s), "moments")
+        _check(cl.cl().mhd_cl_moments(self.raw_t.data_ptr(), 8, S * nv, tsum.data_ptr(), s), "moments")
+        sx, st = sums.cpu().numpy(), tsum.cpu().numpy()
+        cnt = float(S * nv)
+        mean = sx[:8] / cnt
+        std = np.sqrt(np.maximum(sx[8:] / cnt - mean ** 2, 1e-30))
+        trms = np.sqrt(np.maximum(st[8:] / cnt, 1e-30))
+        stats = cl.Stats(mean=mean, inv_std=1.0 / std, oscale=trms[:5], bscale=float(np.sqrt(np.mean(trms[5:] ** 2))))
+        self.x = torch.empty((S, nv * 16), dtype=torch.bfloat16, device="cuda")
+        self.t = torch.empty((S, nv * 8), dtype=torch.bfloat16, device="cuda")
+        f32 = dict(dtype=torch.float32, device="cuda")
+        m_d = torch.tensor(mean, **f32)
+        i_d = torch.tensor(1.0 / std, **f32)
+        tz = torch.zeros(8, **f32)
+        ti = torch.tensor(np.concatenate([1.0 / stats.oscale, np.full(3, 1.0 / stats.bscale)]), **f32)
+        _check(cl.cl().mhd_cl_normalize(self.raw_x.data_ptr(), 8, S * nv, m_d.data_ptr(), i_d.data_ptr(),
+                                        self.x.data_ptr(), 16, s), "normalize x")
+        _check(cl.cl().mhd_cl_normalize(self.raw_t.data_ptr(), 8, S * nv, tz.data_ptr(), ti.data_ptr(),
+                                        self.t.data_ptr(), 8, s), "normalize t")
+        torch.cuda.synchronize()
+        del self.raw_x, self.raw_t
+        self.stats = stats
+        return stats
+
+
+_log = functools.partial(print, flush=True)
+
+
+def generate(runs: int, fine: int = 256, factor: int = 4, samples: int = 20, every: int = 45, seed0: int = 0,
+             cfl: float = 0.7, log=_log) -> Dataset:
+    torch = _torch()
+    nc = fine // factor
+    ds = Dataset(runs * samples, nc)
+    L = cl.cl()
+    ctx_f = Context(fine, fine, fine)
+    ctx_g = Context(fine, fine, fine)
+    ctx_c = Context(nc, nc, nc)
+    f32 = dict(dtype=torch.float32, device="cuda")
+    uc0, bc0 = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    uf1, bf1 = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    ucs, bcs = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    t0 = time.perf_counter()
+    for r in range(runs):
+        u, b = init_vortex(fine, fine, fine, seed=seed0 + r)
+        ctx_f.set_state(u, b)
+        for q in range(samples):
+            if q:
+                ctx_f.step(every, cfl=cfl)
+            ctx_f.sync()
+            fu, fb = ctx_f.state_ptrs()
+            s = cl.stream_ptr()
+            _check(L.mhd_cl_filter(fu, fb, fine, factor, uc0.data_ptr(), bc0.data_ptr(), s), "filter")
+            _check(L.mhd_cl_features(uc0.data_ptr(), bc0.data_ptr(), nc, None, None,
+                                     ds.raw_x[ds.count].data_ptr(), None, s), "features")
+            torch.cuda.synchronize()
+            # one plain coarse step from the filtered state
+            _set_state_dev(ctx_c, uc0.data_ptr(), bc0.data_ptr())
+            ctx_c.step(1, cfl=cfl)
+            tc, _, _ = ctx_c.time()
+            _get_state_dev(ctx_c, ucs, bcs)
+            # the fine run advanced to the same physical time
+            _set_state_dev(ctx_g, fu, fb)
+            tf = tc * factor
+            ctx_g.set_time(0.0, tf)
+            for _ in range(64):
+                ctx_g.step(2, cfl=cfl)
+                if reached(ctx_g.time()[0], tf):
+                    break
+            gu, gb = ctx_g.state_ptrs()
+            s = cl.stream_ptr()
+            _check(L.mhd_cl_filter(gu, gb, fine, factor, uf1.data_ptr(), bf1.data_ptr(), s), "filter")
+            _check(L.mhd_cl_diff(uf1.data_ptr(), bf1.data_ptr(), ucs.data_ptr(), bcs.data_ptr(), nc,
+                                 ds.raw_t[ds.count].data_ptr(), s), "diff")
+            torch.cuda.synchronize()
+            ds.count += 1
+        if log and (r % max(1, runs // 8) == 0 or r == runs - 1):
+            log(f"generate: run {r + 1}/{runs}, {ds.count} samples, {time.perf_counter() - t0:.1f} s")
+    for c in (ctx_f, ctx_g, ctx_c):
+        c.close()
+    return ds
+
+
+def train(ds: Dataset, iters: int = 3000, batch: int = 4, lr: float = 1e-3, seed: int = 0, val_frac: float = 0.05,
+          log=_log):
+    """AdamW with cosine decay on random batches of whole boxes; returns (net, history)."""
+    torch = _torch()
+    n, S = ds.n, ds.count
+    nval = max(1, int(S * val_frac))
+    ntr = S - nval
+    net = cl.ClosureNet(stats=ds.stats, seed=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xb = torch.empty((batch, n ** 3 * 16), dtype=torch.bfloat16, device="cuda")
+    tb = torch.empty((batch, n ** 3 * 8), dtype=torch.bfloat16, device="cuda")
+    hist = []
+    t0 = time.perf_counter()
+    for it in range(iters):
+        idx = torch.from_numpy(rng.integers(0, ntr, size=batch)).to("cuda")
+        torch.index_select(ds.x, 0, idx, out=xb)
+        torch.index_select(ds.t, 0, idx, out=tb)
+        a = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * it / iters)))
+        net.forward(xb, batch, n)
+        net.loss(tb, batch, n)
+        net.backward(xb, batch, n)
+        net.adamw(a)
+        if it % max(1, iters // 20) == 0 or it == iters - 1:
+            tr = net.loss_value()
+            va = validate(net, ds, range(ntr, S))
+            hist.append({"iter": it, "train": tr, "val": va})
+            if log:
+                log(f"train: iter {it} loss {tr:.4f} val {va:.4f} ({time.perf_counter() - t0:.1f} s)")
+    return net, hist
+
+
+def validate(net: cl.ClosureNet, ds: Dataset, idx) -> float:
+    """Mean loss over the given samples (one box at a time)."""
+    tot = 0.0
+    idx = list(idx)
+    for i in idx:
+        net.forward(ds.x[i], 1, ds.n)
+        net.loss(ds.t[i], 1, ds.n)
+        tot += net.loss_value()
+    return tot / max(1, len(idx))
+
+
+def baseline_loss(ds: Dataset, idx) -> float:
+    """The loss of a zero prediction (the plain method) on the same samples."""
+    torch = _torch()
+    t = ds.t[list(idx)].float().reshape(len(list(idx)), -1, 8)
+    # fluid: mean square of the targets; faces: the same (curl of a zero EMF is zero)
+    return float((t ** 2).sum() / (8.0 * t.shape[0] * t.shape[1]))
+
+
+def _run_to(ctx: Context, tf: float, cfl: float, chunk: int, corrector=None, stream=None,
+            max_steps: int = 100000) -> int:
+    """Steps until the clock reaches tf (the last step clamped) or max_steps;
+    returns the step count (max_steps or more: tf not reached).
+
+    With a corrector the net runs on `stream` beside the plain step: the
+    step waits only for the feature kernel (the net's one read of the
+    state), the correction waits for both, the next step for the correction.
+    """
+    torch = _torch()
+    ctx.set_time(0.0, tf)
+    steps = 0
+    cs = torch.cuda.ExternalStream(ctx.stream())
+    while True:
+        if corrector is None:
+            ctx.step(chunk, cfl=cfl)
+            steps += chunk
+        else:
+            up, bp = ctx.state_ptrs()
+            with torch.cuda.stream(stream):
+                stream.wait_stream(cs)
+                corrector.features(up, bp)
+                read = torch.cuda.Event()
+                read.record(stream)
+                corrector.forward()
+            cs.wait_event(read)
+            ctx.step(1, cfl=cfl)
+            with torch.cuda.stream(stream):
+                stream.wait_stream(cs)
+                corrector.apply(up, bp)
+            cs.wait_stream(stream)
+            steps += 1
+        if reached(ctx.time()[0], tf) or steps >= max_steps:
+            return steps
+
+
+def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossings: float = 2.0, cfl: float = 0.7,
+             log=_log) -> dict:
+    torch = _torch()
+    nc = fine // factor
+    L = cl.cl()
+    f32 = dict(dtype=torch.float32, device="cuda")
+    ucr, bcr = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    uci, bci = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    side = torch.cuda.Stream()
+    res = []
+    for seed in seeds:
+        u, b = init_vortex(fine, fine, fine, seed=seed)
+        vr = v_rms(u)
+        tf_fine = crossings * fine / vr  # crossing time L / v_rms in fine grid units
+        # fine plain run
+        with Context(fine, fine, fine) as cf:
+            cf.set_state(u, b)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            st = torch.cuda.ExternalStream(cf.stream())
+            ev[0].record(st)
+            nfine = _run_to(cf, tf_fine, cfl, 4)
+            ev[1].record(st)
+            cf.sync()
+            ms_fine = ev[0].elapsed_time(ev[1])
+            fu, fb = cf.state_ptrs()
+            _check(L.mhd_cl_filter(fu, fb, fine, factor, ucr.data_ptr(), bcr.data_ptr(), cl.stream_ptr()), "filter")
+            torch.cuda.synchronize()
+        # coarse initial state = filtered fine initial state
+        du, db = torch.from_numpy(u).to("cuda"), torch.from_numpy(b).to("cuda")
+        _check(L.mhd_cl_filter(du.data_ptr(), db.data_ptr(), fine, factor, uci.data_ptr(), bci.data_ptr(),
+                               cl.stream_ptr()), "filter")
+        torch.cuda.synchronize()
+        out = {"seed": seed, "v_rms": vr, "t_fine": tf_fine, "fine_steps": nfine, "fine_ms": ms_fine}
+        ref_u, ref_b = ucr.cpu().numpy(), bcr.cpu().numpy()
+        ref_spec = energy_spectra(ref_u, ref_b, nc)
+        for label, use in (("plain", False), ("closure", True)):
+            with Context(nc, nc, nc) as cc:
+                _set_state_dev(cc, uci.data_ptr(), bci.data_ptr())
+                corr = cl.Corrector(net, nc) if use else None
+                st = torch.cuda.ExternalStream(cc.stream())
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                torch.cuda.synchronize()
+                ev[0].record(st)
+                t_host = time.perf_counter()
+                cap = 10000 if not use else 4 * out["plain"]["steps"] + 64
+                nst = _run_to(cc, tf_fine / factor, cfl, 8, corrector=corr, stream=side, max_steps=cap)
+                ev[1].record(st)
+                cc.sync()
+                torch.cuda.synchronize()
+                wall = (time.perf_counter() - t_host) * 1e3
+                cu_, cb_ = cc.get_state()
+                divb = cc.divb_max()
+                done = reached(cc.time()[0], tf_fine / factor)
+            spec = energy_spectra(cu_, cb_, nc)
+            errs = field_errors(cu_, cb_, ref_u, ref_b)
+            U = cu_.reshape(-1, 5)
+            out[label] = {
+                "steps": nst, "ms": ev[0].elapsed_time(ev[1]), "wall_ms": wall, "reached_t": bool(done),
+                "rho_rel_l2": errs["rho"], "field_errors": errs,
+                "kinetic_spectrum_err": spectrum_error(spec["kinetic"], ref_spec["kinetic"], nc // 2),
+                "magnetic_spectrum_err": spectrum_error(spec["magnetic"], ref_spec["magnetic"], nc // 2),
+                "divb_max": divb, "rho_min": float(U[:, 0].min()),
+                "fallbacks": corr.fallback_count() if corr else 0,
+            }
+        out["speedup_vs_fine"] = out["fine_ms"] / max(out["closure"]["wall_ms"], 1e-9)
+        res.append(out)
+        if log:
+            log(f"evaluate: seed {seed} rho L2 plain {out['plain']['rho_rel_l2']:.4f} closure "
+                f"{out['closure']['rho_rel_l2']:.4f}, Emag spec plain {out['plain']['magnetic_spectrum_err']:.4f} "
+                f"closure {out['closure']['magnetic_spectrum_err']:.4f}, fallbacks {out['closure']['fallbacks']}, "
+                f"fine {ms_fine:.0f} ms vs closure {out['closure']['wall_ms']:.0f} ms")
+    keys = ("rho_rel_l2", "kinetic_spectrum_err", "magnetic_spectrum_err")
+    summary = {f"{lab}_{k}": float(np.mean([r[lab][k] for r in res])) for lab in ("plain", "closure") for k in keys}
+    summary["fallback_rate"] = float(np.sum([r["closure"]["fallbacks"] for r in res]) /
+                                     max(1, np.sum([r["closure"]["steps"] for r in res])))
+    summary["speedup_vs_fine"] = float(np.mean([r["speedup_vs_fine"] for r in res]))
+    return {"seeds": list(seeds), "fine": fine, "coarse": nc, "crossings": crossings, "summary": summary, "runs": res}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--runs", type=int, default=48)
+    ap.add_argument("--fine", type=int, default=256)
+    ap.add_argument("--factor", type=int, default=4)
+    ap.add_argument("--samples", type=int, default=20)
+    ap.add_argument("--every", type=int, default=45)
+    ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--eval-seeds", type=int, nargs="*", default=list(range(1000, 1008)))
+    ap.add_argument("--crossings", type=float, default=2.0)
+    ap.add_argument("--model", default="closure_model.npz")
+    ap.add_argument("--load", default=None, help="skip data and training, evaluate this model")
+    ap.add_argument("--report", default="closure_report.json")
+    a = ap.parse_args(argv)
+    report = {"args": vars(a)}
+    if a.load:
+        net = cl.ClosureNet.load(a.load)
+    else:
+        t0 = time.perf_counter()
+        ds = generate(a.runs, a.fine, a.factor, a.samples, a.every)
+        stats = ds.finalize()
+        report["generate_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        net, hist = train(ds, a.iters, a.batch, a.lr)
+        report["train_s"] = time.perf_counter() - t0
+        nval = max(1, int(ds.count * 0.05))
+        report["history"] = hist
+        report["val_loss"] = validate(net, ds, range(ds.count - nval, ds.count))
+        report["val_loss_plain"] = baseline_loss(ds, range(ds.count - nval, ds.count))
+        report["stats"] = stats.to_json()
+        net.save(a.model)
+        del ds
+    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings)
+    with open(a.report, "w") as f:
+        json.dump(report, f, indent=1)
+    print(json.dumps(report["evaluation"]["summary"]))
+
+
+if __name__ == "__main__":
+    main()

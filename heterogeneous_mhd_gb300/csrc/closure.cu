@@ -615,13 +615,34 @@ __global__ void k_diff(const float* __restrict__ ua, const float* __restrict__ b
 
 // ------------------------------------------------------------ correction step
 
-// candidate = state + correction into (ut, bt); flags |= 1 for rho <= 0 or p <= 0 (or non-finite),
+// esum[2 + c] += sum over the box of out[.][c], c < 5 (the fluid corrections' means are removed,
+// so the correction conserves mass, momentum and energy as the filtered fine step does)
+__global__ void k_apply0(const float* __restrict__ out, size_t nv, double* __restrict__ esum)
+{
+    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int c = 0; c < 5; c++)
+            s[c] += out[v * 8 + c];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        const double t = mhd_warp_sum_d(s[c]);
+        if ((threadIdx.x & 31) == 0)
+            atomicAdd(&esum[2 + c], t);
+    }
+}
+
+// candidate = state + correction (fluid part with its box mean removed) into (ut, bt);
 // esum[0] += sum E, esum[1] += sum E of the candidate
 __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ b, const float* __restrict__ out,
                          int n, const float* __restrict__ oscale, float bscale, float* __restrict__ ut,
                          float* __restrict__ bt, double* __restrict__ esum)
 {
     const size_t nv = (size_t)n * n * n;
+    float mean[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++)
+        mean[q] = (float)(esum[2 + q] / (double)nv);
     double e0 = 0.0, e1 = 0.0;
     for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(v % n), j = (int)((v / n) % n), k = (int)(v / ((size_t)n * n));
@@ -631,7 +652,7 @@ __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ 
         const float* ok = out + vidx(0, k + 1 == n ? 0 : k + 1, j, i, n) * 8;
 #pragma unroll
         for (int q = 0; q < 5; q++)
-            ut[v * 5 + q] = u[v * 5 + q] + oscale[q] * o[q];
+            ut[v * 5 + q] = u[v * 5 + q] + oscale[q] * (o[q] - mean[q]);
         bt[v * 3] = b[v * 3] + bscale * (-(oj[7] - o[7]) + (ok[6] - o[6]));
         bt[v * 3 + 1] = b[v * 3 + 1] + bscale * (-(ok[5] - o[5]) + (oi[7] - o[7]));
         bt[v * 3 + 2] = b[v * 3 + 2] + bscale * (-(oi[6] - o[6]) + (oj[5] - o[5]));
@@ -951,9 +972,10 @@ extern "C" MHD_API int mhd_cl_apply(float* u, float* b, const float* out, int n,
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t nv = (size_t)n * n * n;
     if (cudaMemsetAsync(flags, 0, sizeof(int), s) != cudaSuccess ||
-        cudaMemsetAsync(esum, 0, 2 * sizeof(double), s) != cudaSuccess)
+        cudaMemsetAsync(esum, 0, 8 * sizeof(double), s) != cudaSuccess)
         return MHD_ERR_CUDA;
     const unsigned blocks = blocks_for(nv, 256);
+    k_apply0<<<blocks, 256, 0, s>>>(out, nv, esum);
     k_apply1<<<blocks, 256, 0, s>>>(u, b, out, n, oscale, bscale, u_tmp, b_tmp, esum);
     k_apply2<<<blocks, 256, 0, s>>>(u_tmp, b_tmp, n, flags);
     k_apply3<<<blocks, 256, 0, s>>>(u, b, u_tmp, b_tmp, nv, flags, esum, ecap, fallbacks);

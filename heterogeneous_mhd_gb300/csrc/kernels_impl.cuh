@@ -77,21 +77,73 @@ static FxPlan plan_fluidx(int nx, int ny, bool aligned)
     return p;
 }
 
-template <int C, int T>
+template <int C, int T, int AX = 0>
 static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T>, attr, true);
+    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T, AX>, attr, AX == 0);
     if (e != cudaSuccess)
         return e;
-    dim3 grid(a.ny / a.P, a.nz, a.bs.count);
-    k_fluidx2<R, EX, C, T><<<grid, a.P * T, fluidx2_smem_elems(a.nx, a.P) * sizeof(R), s>>>(a);
+    // grid: (pencil groups along j, planes along k, boxes)
+    const int nj = (AX == 0) ? a.ny : a.nx, nk = (AX == 2) ? a.ny : a.nz;
+    dim3 grid(nj / a.P, nk, a.bs.count);
+    k_fluidx2<R, EX, C, T, AX><<<grid, a.P * T, fluidx2_smem_elems(C * T, a.P, AX) * sizeof(R), s>>>(a);
     return cudaGetLastError();
+}
+
+// Sweep of the untransposed state along y or z (fused step): the pencil
+// length is ny or nz, P pencils at consecutive x per CTA.
+static bool plan_fluidx_sweep(int n, int nx, FxPlan& p)
+{
+    p = FxPlan{0, 0, 0};
+    if (!kV2)
+        return false;
+    if (n % 4 == 0 && pow2_in(n / 4, 8, 128))
+        p.C = 4, p.T = n / 4;
+    else if (n % 3 == 0 && n % 4 == 0 && pow2_in(n / 3, 16, 128))
+        p.C = 3, p.T = n / 3;
+    else
+        return false;
+    for (int P = 1; P <= 8 && P <= nx; P++)
+        if (nx % P == 0 && P * p.T <= 256 && (P * p.T) % 32 == 0)
+            p.P = P;
+    return p.P > 0;
+}
+
+template <int AX>
+static cudaError_t fluidx_sweep(FluidxArgs a, const FxPlan& p, cudaStream_t s)
+{
+    if constexpr (kV2) {
+        a.P = p.P;
+        if (p.C == 4) {
+            switch (p.T) {
+            case 8: return launch_fx2<4, 8, AX>(a, s);
+            case 16: return launch_fx2<4, 16, AX>(a, s);
+            case 32: return launch_fx2<4, 32, AX>(a, s);
+            case 64: return launch_fx2<4, 64, AX>(a, s);
+            case 128: return launch_fx2<4, 128, AX>(a, s);
+            }
+        } else {
+            switch (p.T) {
+            case 16: return launch_fx2<3, 16, AX>(a, s);
+            case 32: return launch_fx2<3, 32, AX>(a, s);
+            case 64: return launch_fx2<3, 64, AX>(a, s);
+            case 128: return launch_fx2<3, 128, AX>(a, s);
+            }
+        }
+    }
+    return cudaErrorInvalidValue;
 }
 
 static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
 {
     FluidxArgs a = in;
+    if (a.axis != 0) {
+        FxPlan p;
+        if (a.cfl_part || !plan_fluidx_sweep(a.axis == 1 ? a.ny : a.nz, a.nx, p))
+            return cudaErrorInvalidValue;
+        return (a.axis == 1) ? fluidx_sweep<1>(a, p, s) : fluidx_sweep<2>(a, p, s);
+    }
     const FxPlan p = plan_fluidx(a.nx, a.ny, a.use_tma != 0);
     a.P = p.P;
     if constexpr (kV2) {
@@ -160,7 +212,7 @@ struct A3Plan {
     int C, T, NS, J, K;
 };
 
-static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p)
+static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax = 0)
 {
     if (!kV2 || !aligned)
         return false;
@@ -176,10 +228,10 @@ static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p)
     const int jt = tune_value(TUNE_ADVECT_J);
     p.J = 0;
     for (int j = 1; j <= ny && j <= 16; j++) {
-        const bool fits = advect3_threads(j, p.T) <= 384 && advect3_smem_floats(j, nx, p.NS) * sizeof(float) <= 227 * 1024;
+        const bool fits = advect3_threads(j, p.T) <= 384 && advect3_smem_floats(j, nx, p.NS, ax) * sizeof(float) <= 227 * 1024;
         if (ny % j != 0 || !fits)
             continue;
-        if (jt ? (j == jt) : (advect3_smem_floats(j, nx, p.NS) * sizeof(float) <= smem_cap))
+        if (jt ? (j == jt) : (advect3_smem_floats(j, nx, p.NS, ax) * sizeof(float) <= smem_cap))
             p.J = j;
     }
     if (!p.J)
@@ -195,30 +247,40 @@ static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p)
     return true;
 }
 
-template <int C, int T, int NS>
+template <int C, int T, int NS, int AX = 0>
 static cudaError_t launch_ad3(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    cudaError_t e = allow_smem(k_advect3<EX, C, T, NS>, attr, true);
+    cudaError_t e = allow_smem(k_advect3<EX, C, T, NS, AX>, attr, AX == 0);
     if (e != cudaSuccess)
         return e;
-    dim3 grid(a.ny / a.P, a.nz / a.K, a.bs.count);
-    k_advect3<EX, C, T, NS><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, a.nx, NS) * sizeof(float), s>>>(a);
+    const int nj = (AX == 0) ? a.ny : a.nx, nk = (AX == 2) ? a.ny : a.nz;
+    dim3 grid(nj / a.P, nk / a.K, a.bs.count);
+    k_advect3<EX, C, T, NS, AX><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, C * T, NS, AX) * sizeof(float),
+                                  s>>>(a);
     return cudaGetLastError();
 }
 
-template <int C, int NS>
+template <int C, int NS, int AX = 0>
 static cudaError_t launch_ad3_t(const AdvectArgs& a, int T, cudaStream_t s)
 {
     switch (T) {
-    case 4: if constexpr (C == 8) return launch_ad3<C, 4, NS>(a, s); break;
-    case 8: return launch_ad3<C, 8, NS>(a, s);
-    case 16: return launch_ad3<C, 16, NS>(a, s);
-    case 32: return launch_ad3<C, 32, NS>(a, s);
-    case 64: return launch_ad3<C, 64, NS>(a, s);
-    case 128: if constexpr (C == 4) return launch_ad3<C, 128, NS>(a, s); break;
+    case 4: if constexpr (C == 8) return launch_ad3<C, 4, NS, AX>(a, s); break;
+    case 8: return launch_ad3<C, 8, NS, AX>(a, s);
+    case 16: return launch_ad3<C, 16, NS, AX>(a, s);
+    case 32: return launch_ad3<C, 32, NS, AX>(a, s);
+    case 64: return launch_ad3<C, 64, NS, AX>(a, s);
+    case 128: if constexpr (C == 4) return launch_ad3<C, 128, NS, AX>(a, s); break;
     }
     return cudaErrorInvalidValue;
+}
+
+template <int AX>
+static cudaError_t advect_sweep(const AdvectArgs& a, const A3Plan& p3, cudaStream_t s)
+{
+    if (p3.C == 4)
+        return (p3.NS == 2) ? launch_ad3_t<4, 2, AX>(a, p3.T, s) : launch_ad3_t<4, 3, AX>(a, p3.T, s);
+    return (p3.NS == 2) ? launch_ad3_t<8, 2, AX>(a, p3.T, s) : launch_ad3_t<8, 3, AX>(a, p3.T, s);
 }
 
 template <int C, int T>
@@ -236,6 +298,15 @@ static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
 static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
 {
     AdvectArgs a = in;
+    if (a.axis != 0) {  // fused step: pencils along y or z of the untransposed state
+        A3Plan p3;
+        const int n = (a.axis == 1) ? a.ny : a.nz, nk = (a.axis == 1) ? a.nz : a.ny;
+        if (!kV2 || a.b1_src != a.ub || !plan_advect3(n, a.nx, nk, true, p3, a.axis))
+            return cudaErrorInvalidValue;
+        a.P = p3.J;
+        a.K = p3.K;
+        return (a.axis == 1) ? advect_sweep<1>(a, p3, s) : advect_sweep<2>(a, p3, s);
+    }
     const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
                          reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
     if constexpr (kV2) {
@@ -341,8 +412,17 @@ static cudaError_t divb(const void* b, int nx, int ny, int nz, double* part, int
     return cudaGetLastError();
 }
 
+// the fused step's sweeps along y and z have kernels for this shape
+static int fused_ok(int nx, int ny, int nz)
+{
+    FxPlan p;
+    A3Plan q;
+    return plan_fluidx_sweep(ny, nx, p) && plan_fluidx_sweep(nz, nx, p) && plan_advect3(ny, nx, nz, true, q, 1) &&
+           plan_advect3(nz, nx, ny, true, q, 2);
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
-                               sizeof(CflPart<R>), fluidx_parts};
+                               sizeof(CflPart<R>), fluidx_parts, fused_ok};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

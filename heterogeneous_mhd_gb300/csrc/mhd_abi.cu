@@ -307,7 +307,7 @@ extern "C" MHD_API int mhd_sync(mhd_ctx* c)
 // ------------------------------------------------------------ operators
 
 static int op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx, int ny, int nz, double dt,
-                     const void* dt_dev, void* cfl_part)
+                     const void* dt_dev, void* cfl_part, int axis = 0)
 {
     MHD_TRY(check_dims(nx, ny, nz));
     FluidxArgs a{};
@@ -325,13 +325,14 @@ static int op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx
     a.dt_ptr = dt_dev;
     a.cfl_part = cfl_part;
     a.err = c->err_dev;
+    a.axis = axis;
     KTimer kt(c, MHD_K_FLUIDX);
     CUDA_TRY(c->ks->fluidx(a, c->stream));
     return MHD_OK;
 }
 
 static int op_advect(mhd_ctx* c, void* b_out, const void* b1_src, const void* uu, const void* ub, int nx, int ny,
-                     int nz, double dt, const void* dt_dev)
+                     int nz, double dt, const void* dt_dev, int axis = 0)
 {
     MHD_TRY(check_dims(nx, ny, nz));
     AdvectArgs a{};
@@ -346,6 +347,7 @@ static int op_advect(mhd_ctx* c, void* b_out, const void* b1_src, const void* uu
     a.dt_val = dt;
     a.dt_ptr = dt_dev;
     a.err = c->err_dev;
+    a.axis = axis;
     KTimer kt(c, MHD_K_ADVECT);
     CUDA_TRY(c->ks->advect(a, c->stream));
     return MHD_OK;
@@ -645,6 +647,46 @@ static int enqueue_plain_step(mhd_ctx* c, double cfl)
     return MHD_OK;
 }
 
+// One fused Strang step on (U0,B0) -> (U0,B0): the same operator sequence
+// as the plain step with every transpose removed; the sweeps along y and z
+// read the untransposed state and see it in the transposed component order,
+// so each operator computes what the plain step's operator computes on the
+// transposed arrays, and the results are identical.
+static int enqueue_fused_step(mhd_ctx* c, double cfl)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    void *U0 = c->U[0].p, *U1 = c->U[1].p, *B0 = c->B[0].p, *B1 = c->B[1].p;
+    const void* dt = static_cast<char*>(c->clock.p) + 2 * c->elem;
+    MHD_TRY(op_finalize(c, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
+    // x
+    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 0));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 0));
+    // y
+    MHD_TRY(op_fluidx(c, U0, U1, B1, nx, ny, nz, 0, dt, nullptr, 1));
+    MHD_TRY(op_advect(c, B0, B1, U0, B1, nx, ny, nz, 0, dt, 1));
+    // z, z
+    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 2));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 2));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 2));
+    MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, nullptr, 2));
+    // y
+    MHD_TRY(op_advect(c, B1, B0, U0, B0, nx, ny, nz, 0, dt, 1));
+    MHD_TRY(op_fluidx(c, U1, U0, B1, nx, ny, nz, 0, dt, nullptr, 1));
+    // x, with the calcfl epilogue for the next step
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0));
+    const size_t nparts = fluidx_parts(c);
+    if (c->part.cap < nparts * c->ks->part_bytes)
+        return MHD_ERR_ARG;
+    MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, c->part.p, 0));
+    c->cfl_nparts = (int)nparts;
+    return MHD_OK;
+}
+
+static int enqueue_step(mhd_ctx* c, double cfl, int variant)
+{
+    return variant == MHD_FUSED ? enqueue_fused_step(c, cfl) : enqueue_plain_step(c, cfl);
+}
+
 static int ensure_cfl(mhd_ctx* c)
 {
     if (c->cfl_valid)
@@ -660,9 +702,8 @@ static int ensure_cfl(mhd_ctx* c)
 
 static int step_once_direct(mhd_ctx* c, double cfl, int variant)
 {
-    (void)variant;
     MHD_TRY(ensure_cfl(c));
-    MHD_TRY(enqueue_plain_step(c, cfl));
+    MHD_TRY(enqueue_step(c, cfl, variant));
     return MHD_OK;
 }
 
@@ -683,7 +724,7 @@ static int step_graph(mhd_ctx* c, double cfl, int variant)
         CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         c->capturing = true;
         const long long before = c->launch_count;
-        int s = enqueue_plain_step(c, cfl);
+        int s = enqueue_step(c, cfl, variant);
         c->capturing = false;
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         c->launch_count = before;  // counted per replay below
@@ -711,7 +752,9 @@ extern "C" MHD_API int mhd_step(mhd_ctx* c, int nsteps, double cfl, int variant)
 {
     if (!c || !c->have_state || nsteps < 0 || !(cfl > 0) || (variant != MHD_PLAIN && variant != MHD_FUSED))
         return set_err(MHD_ERR_ARG);
-    if (c->ny != c->nz)  // transpose13 is applied to (ny,nx,nz) and (nz,nx,ny)
+    if (variant == MHD_PLAIN && c->ny != c->nz)  // transpose13 is applied to (ny,nx,nz) and (nz,nx,ny)
+        return set_err(MHD_ERR_UNSUPPORTED);
+    if (variant == MHD_FUSED && !c->ks->fused_ok(c->nx, c->ny, c->nz))
         return set_err(MHD_ERR_UNSUPPORTED);
     MHD_TRY(set_err(check_dims(c->nx, c->ny, c->nz)));
     MHD_TRY(set_err(check_dims(c->ny, c->nx, c->nz)));

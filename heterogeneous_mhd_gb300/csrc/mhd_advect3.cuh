@@ -16,6 +16,14 @@
 // Every input pencil is read from global memory once per CTA and every B row
 // is computed once (one extra plane of B rows per K planes).  With C = 4 the
 // 20-word thread chunks are read without bank conflicts.
+//
+// AX = 1, 2: the same operator along y or z of the untransposed state (the
+// fused step): pencils along the sweep axis, j = x, k = z (AX = 1) or y
+// (AX = 2).  A plane slab is gathered from its rows (the J+2 cells at
+// consecutive x, contiguous in HBM) word by word over consecutive threads
+// into the same pencil-major layout (pencil stride padded by kSweepPad) by
+// 4-byte cp.async, with the components seen in the transposed order; the
+// combined b pencils are staged in shared memory and written back as rows.
 #pragma once
 #include "mhd_advect2.cuh"
 
@@ -30,14 +38,17 @@ __host__ __device__ inline int advect3_threads(int J, int T)
 }
 
 // shared memory in floats: NS u slabs, NS b slabs, FA[J+1][n], FB[2][J][n],
-// B3[2][J][n], seam; plus the mbarriers (in the static part)
-__host__ __device__ inline size_t advect3_smem_floats(int J, int n, int NS)
+// B3[2][J][n], seam, and for the y/z sweeps the output rows [J][n][3]; plus
+// the mbarriers (in the static part)
+__host__ __device__ inline size_t advect3_smem_floats(int J, int n, int NS, int ax = 0)
 {
-    const size_t uslab = (size_t)(J + 2) * n * 5, bslab = (size_t)(J + 1) * n * 3;
-    return NS * uslab + NS * bslab + (size_t)(J + 1) * n + (size_t)4 * J * n + 2 * 32 * kSeamVals;
+    const size_t pad = ax ? kSweepPad : 0;
+    const size_t uslab = (size_t)(J + 2) * (n * 5 + pad), bslab = (size_t)(J + 1) * (n * 3 + pad);
+    return NS * uslab + NS * bslab + (size_t)(J + 1) * n + (size_t)4 * J * n + 2 * 32 * kSeamVals +
+           (ax ? (size_t)J * (3 * n + pad) : 0);
 }
 
-template <bool EX, int C, int T, int NS>
+template <bool EX, int C, int T, int NS, int AX = 0>
 __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
 {
     select_box(a, blockIdx.z);
@@ -53,11 +64,12 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     const bool live = r < NR;
     if (!live)
         r = 0;
-    const int ny = a.ny, nz = a.nz;
+    // sizes of the j and k axes (j = y, k = z for the x sweep; j = x otherwise)
+    const int ny = (AX == 0) ? a.ny : a.nx, nz = (AX == 0) ? a.nz : (AX == 1 ? a.nz : a.ny);
     const int j0 = blockIdx.x * J, k0 = blockIdx.y * K;
     const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
 
-    constexpr int UROW = n * 5, BROW = n * 3;  // words per pencil row
+    constexpr int UROW = n * 5 + (AX ? kSweepPad : 0), BROW = n * 3 + (AX ? kSweepPad : 0);  // pencil strides
     const size_t uslab = (size_t)(J + 2) * UROW, bslab = (size_t)(J + 1) * BROW;
     float* U = reinterpret_cast<float*>(smem_raw);  // [NS][J+2][n*5]
     float* B = U + NS * uslab;                        // [NS][J+1][n*3]
@@ -65,6 +77,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     float* FB = FA + (size_t)(J + 1) * n;             // [2][J][n]
     float* B3 = FB + (size_t)2 * J * n;               // [2][J][n]
     float* seam = B3 + (size_t)2 * J * n;
+    float* SO = seam + 2 * 32 * kSeamVals;            // [J][BROW] output pencils (AX != 0)
 
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
@@ -72,23 +85,55 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     // ---- slab loads: plane p into ring slot s (one mbarrier per slot),
     // issued by warp 0: lane 0 registers the bytes, one lane per pencil copies.
     auto load_plane = [&](int p, int s) {
-        if (tid < 32) {
-            const int pp = ((p % nz) + nz) % nz;
-            if (tid == 0)
-                mbar_arrive_expect_tx(&bar[s], (uint32_t)((J + 2) * n * 20 + (J + 1) * n * 12));
-            __syncwarp();
-            for (int row = tid; row < J + 2; row += 32) {
-                int j = j0 - 1 + row;
-                j = (j < 0) ? j + ny : (j >= ny ? j - ny : j);
-                const size_t cell = ((size_t)pp * ny + j) * n;
-                tma_load_1d(U + s * uslab + (size_t)row * UROW, uu + cell * 5, n * 20, &bar[s]);
+        const int pp = ((p % nz) + nz) % nz;
+        if constexpr (AX == 0) {
+            if (tid < 32) {
+                if (tid == 0)
+                    mbar_arrive_expect_tx(&bar[s], (uint32_t)((J + 2) * n * 20 + (J + 1) * n * 12));
+                __syncwarp();
+                for (int row = tid; row < J + 2; row += 32) {
+                    int j = j0 - 1 + row;
+                    j = (j < 0) ? j + ny : (j >= ny ? j - ny : j);
+                    const size_t cell = ((size_t)pp * ny + j) * n;
+                    tma_load_1d(U + s * uslab + (size_t)row * UROW, uu + cell * 5, n * 20, &bar[s]);
+                }
+                for (int row = tid; row < J + 1; row += 32) {
+                    int j = j0 + row;
+                    j = (j >= ny) ? j - ny : j;
+                    const size_t cell = ((size_t)pp * ny + j) * n;
+                    tma_load_1d(B + s * bslab + (size_t)row * BROW, ub + cell * 3, n * 12, &bar[s]);
+                }
             }
-            for (int row = tid; row < J + 1; row += 32) {
-                int j = j0 + row;
-                j = (j >= ny) ? j - ny : j;
-                const size_t cell = ((size_t)pp * ny + j) * n;
-                tma_load_1d(B + s * bslab + (size_t)row * BROW, ub + cell * 3, n * 12, &bar[s]);
+        } else {
+            // rows of u at x0-1..x0+J and of b at x0..x0+J, position i of plane pp,
+            // word by word over consecutive threads
+            for (RowIter it(tid, blockDim.x, 5 * (J + 2)); it.row < n; it.next()) {
+                const int pj = it.w / 5, c = it.w - 5 * pj;
+                int x = j0 - 1 + pj;
+                x = (x < 0) ? x + ny : (x >= ny ? x - ny : x);
+                cp_async4(U + s * uslab + (size_t)pj * UROW + it.row * 5 + c,
+                          uu + sweep_cell<AX>(it.row, x, pp, a.nx, a.ny) * 5 + c);
             }
+            for (RowIter it(tid, blockDim.x, 3 * (J + 1)); it.row < n; it.next()) {
+                const int pj = it.w / 3, c = it.w - 3 * pj;
+                int x = j0 + pj;
+                x = (x >= ny) ? x - ny : x;
+                cp_async4(B + s * bslab + (size_t)pj * BROW + it.row * 3 + c,
+                          ub + sweep_cell<AX>(it.row, x, pp, a.nx, a.ny) * 3 + c);
+            }
+            cp_async_commit();
+        }
+    };
+    // wait for the slab of a plane; `later` = planes requested after it (0 or 1)
+    auto wait_plane = [&](int p, int later) {
+        if constexpr (AX == 0) {
+            mbar_wait_bounded(&bar[(p - k0 + 1) % NS], (uint32_t)(((p - k0 + 1) / NS) & 1), a.err);
+        } else {
+            if (later)
+                cp_async_wait<1>();
+            else
+                cp_async_wait<0>();
+            __syncthreads();
         }
     };
     // ring slot and mbarrier parity of plane p (slot 0 gets k0-1, k0-1+NS, ...)
@@ -103,10 +148,11 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         lds_chunk<float, C * 3>(B + s * bslab + (size_t)row * BROW + g.t * C * 3, out);
     };
     // raw face velocity between two u chunks (C/advectbyzxA1.c:34, C/advectbyzxB1.c:34)
+    constexpr int UM = sweep_u<AX>(1), BD = sweep_b<AX>(0), BJ = sweep_b<AX>(1), BK = sweep_b<AX>(2);
     auto face_v = [&](const float (&um)[C * 5], const float (&uc)[C * 5], float (&vr)[C]) {
 #pragma unroll
         for (int m = 0; m < C; m++) {
-            const float num = um[5 * m + 1] + uc[5 * m + 1], den = um[5 * m] + uc[5 * m];
+            const float num = um[5 * m + UM] + uc[5 * m + UM], den = um[5 * m] + uc[5 * m];
             if constexpr (EX)
                 vr[m] = num / den;
             else
@@ -114,7 +160,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         }
     };
 
-    if (tid == 0)
+    if (AX == 0 && tid == 0)
         for (int s = 0; s < NS; s++)
             mbar_init(&bar[s], 1);
     __syncthreads();
@@ -122,8 +168,8 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     load_plane(k0, slot_of(k0));
     if (NS >= 3)
         load_plane(k0 + 1, slot_of(k0 + 1));
-    mbar_wait_bounded(&bar[slot_of(k0 - 1)], parity_of(k0 - 1), a.err);
-    mbar_wait_bounded(&bar[slot_of(k0)], parity_of(k0), a.err);
+    wait_plane(k0 - 1, 1);
+    wait_plane(k0, NS >= 3 ? 1 : 0);
 
     // ---- prologue: B rows of plane k0 (FB and advected b(3) of the first step)
     const bool brow = live && r > J;  // B-row groups: pencil j0 + (r-J-1)
@@ -138,7 +184,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         face_v(um, uc, vr);
 #pragma unroll
         for (int m = 0; m < C; m++)
-            bv[m] = bb[3 * m + 2];
+            bv[m] = bb[3 * m + BK];
         tvdb_row<R, EX, C, T>(g, vr, bv, dt, seam, F, bn);
         if (brow) {
             const int pb = k0 & 1;
@@ -165,7 +211,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
             fence_proxy_async_smem();
             load_plane(k + 2, slot_of(k + 2));
         }
-        mbar_wait_bounded(&bar[sk1], parity_of(k + 1), a.err);
+        wait_plane(k + 1, (NS >= 3 && k + 2 <= k0 + K) ? 1 : 0);
         // ---- rows: A at plane k (r <= J), B at plane k+1 (r > J)
         float F[C], bn[C], b1own[C];
         {
@@ -182,8 +228,8 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
             face_v(um, uc, vr);
 #pragma unroll
             for (int m = 0; m < C; m++) {
-                bv[m] = (r <= J) ? bb[3 * m + 1] : bb[3 * m + 2];
-                b1own[m] = bb[3 * m];
+                bv[m] = (r <= J) ? bb[3 * m + BJ] : bb[3 * m + BK];
+                b1own[m] = bb[3 * m + BD];
             }
             tvdb_row<R, EX, C, T>(g, vr, bv, dt, seam, F, bn);
         }
@@ -202,7 +248,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         // ---- combine and store the owned pencils (A-row groups 0..J-1)
         if (live && r < J) {
             const size_t cell0 = ((size_t)(k % nz) * ny + j0 + r) * n + g.t * C;
-            if (b1s != ub) {
+            if (AX == 0 && b1s != ub) {
                 float b1c[C * 3];
                 ldg_chunk<float, C * 3>(b1s + cell0 * 3, b1c);
 #pragma unroll
@@ -221,11 +267,22 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
                 x = x + fa1[m];
                 x = x - fb[m];
                 x = x + fbp[m];
-                out[3 * m] = x;
-                out[3 * m + 1] = bn[m];
-                out[3 * m + 2] = b3[m];
+                out[3 * m + BD] = x;
+                out[3 * m + BJ] = bn[m];
+                out[3 * m + BK] = b3[m];
             }
-            stg_chunk<float, C * 3>(bo + cell0 * 3, out);
+            if constexpr (AX == 0)
+                stg_chunk<float, C * 3>(bo + cell0 * 3, out);
+            else
+                sts_chunk<float, C * 3>(SO + (size_t)r * BROW + (size_t)g.t * C * 3, out);
+        }
+        if constexpr (AX != 0) {  // the J combined pencils back as rows of consecutive x
+            __syncthreads();
+            const int pk_ = k % nz;
+            for (RowIter it(tid, blockDim.x, 3 * J); it.row < n; it.next()) {
+                const int p = it.w / 3, c = it.w - 3 * p;
+                bo[sweep_cell<AX>(it.row, j0, pk_, a.nx, a.ny) * 3 + it.w] = SO[(size_t)p * BROW + it.row * 3 + c];
+            }
         }
         // the B rows' advected b(3) of plane k+1, for the next step
         if (brow) {

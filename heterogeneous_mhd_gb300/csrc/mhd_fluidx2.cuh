@@ -5,6 +5,15 @@
 // update runs in registers: the two pencil maxima are shuffle reductions and
 // the five neighbour exchanges of the stencil are shuffles.  The new u goes
 // back through shared memory and one bulk TMA store.
+//
+// AX = 1, 2: the same sweep along y or z of the untransposed state (the fused
+// step's replacement for transpose12/13 + fluidx + transpose back).  The CTA
+// owns P pencils at consecutive x; the rows (the P cells at one position
+// along the sweep, contiguous in x) are read word by word by consecutive
+// threads into the pencil-major shared layout the engine reads (pencil stride
+// padded by kSweepPad), the components seen in the order the transposed call
+// would see them (C/transpose12.c:7-47, C/transpose13.c:9-62), and the new
+// rows go back the same way.  The arithmetic is the x sweep's.
 #pragma once
 #include "mhd_kernels.cuh"
 #include "mhd_pencil.cuh"
@@ -16,15 +25,16 @@ struct Fx2Shape {
     static constexpr int N = C * T;  // cells per pencil
 };
 
-// shared memory (elements of R): su 5nP, sb 3n(P+1), sbk 3nP, red 32, seam 2*32*10
-__host__ __device__ inline size_t fluidx2_smem_elems(int n, int P)
+// shared memory (elements of R): su P pencils of 5n, sb P+1 pencils of 3n, sbk P of 3n, red 32,
+// seam 2*32*10; the y/z sweeps pad each pencil by kSweepPad
+__host__ __device__ inline size_t fluidx2_smem_elems(int n, int P, int ax = 0)
 {
-    const size_t np = (size_t)n * P;
-    return 5 * np + 3 * (np + n) + 3 * np + 32 + 2 * 32 * 10;
+    const size_t su = 5 * (size_t)n + (ax ? kSweepPad : 0), sb = 3 * (size_t)n + (ax ? kSweepPad : 0);
+    return P * su + (P + 1) * sb + P * sb + 32 + 2 * 32 * 10;
 }
 
-template <typename R, bool EX, int C, int T>
-__global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
+template <typename R, bool EX, int C, int T, int AX = 0>
+__global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
 {
     select_box(a, blockIdx.z, sizeof(CflPart<R>));
     constexpr int n = C * T;
@@ -39,10 +49,11 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
     const int kp = (k + 1 == a.nz) ? 0 : k + 1;
     const int jn = (j0 + P == a.ny) ? 0 : j0 + P;
 
+    constexpr int SU = 5 * n + (AX ? kSweepPad : 0), SB = 3 * n + (AX ? kSweepPad : 0);  // pencil strides
     R* su = reinterpret_cast<R*>(smem_raw);
-    R* sb = su + 5 * np;
-    R* sbk = sb + 3 * (np + n);
-    R* red = sbk + 3 * np;
+    R* sb = su + P * SU;
+    R* sbk = sb + (P + 1) * SB;
+    R* red = sbk + P * SB;
     R* seam = red + 32;
     __shared__ uint64_t bar;
 
@@ -52,17 +63,39 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
     const size_t cn = ((size_t)k * a.ny + jn) * n;
     const size_t ck = ((size_t)kp * a.ny + j0) * n;
 
-    if (tid == 0) {
-        mbar_init(&bar, 1);
-        const uint32_t bu = 5u * np * sizeof(R), bg = 3u * np * sizeof(R), b1 = 3u * n * sizeof(R);
-        mbar_arrive_expect_tx(&bar, bu + 2 * bg + b1);
-        tma_load_1d(su, uu + c0 * 5, bu, &bar);
-        tma_load_1d(sb, ub + c0 * 3, bg, &bar);
-        tma_load_1d(sb + 3 * np, ub + cn * 3, b1, &bar);
-        tma_load_1d(sbk, ub + ck * 3, bg, &bar);
+    if constexpr (AX == 0) {
+        if (tid == 0) {
+            mbar_init(&bar, 1);
+            const uint32_t bu = 5u * np * sizeof(R), bg = 3u * np * sizeof(R), b1 = 3u * n * sizeof(R);
+            mbar_arrive_expect_tx(&bar, bu + 2 * bg + b1);
+            tma_load_1d(su, uu + c0 * 5, bu, &bar);
+            tma_load_1d(sb, ub + c0 * 3, bg, &bar);
+            tma_load_1d(sb + 3 * np, ub + cn * 3, b1, &bar);
+            tma_load_1d(sbk, ub + ck * 3, bg, &bar);
+        }
+        __syncthreads();
+        mbar_wait_bounded(&bar, 0, a.err);
+    } else {
+        // rows of P cells (x0..x0+P-1) at plane k and k+1, and the b of x0+P;
+        // consecutive threads read consecutive words of a row
+        const int x0 = blockIdx.x * P, kk = blockIdx.y;
+        const int nk = (AX == 1) ? a.nz : a.ny;
+        const int kn = (kk + 1 == nk) ? 0 : kk + 1;
+        const int xn = (x0 + P == a.nx) ? 0 : x0 + P;
+        const int nt = blockDim.x;
+        for (RowIter it(tid, nt, 5 * P); it.row < n; it.next()) {
+            const int p = it.w / 5, c = it.w - 5 * p;
+            su[p * SU + it.row * 5 + c] = uu[sweep_cell<AX>(it.row, x0, kk, a.nx, a.ny) * 5 + it.w];
+        }
+        for (RowIter it(tid, nt, 3 * P); it.row < n; it.next()) {
+            const int p = it.w / 3, c = it.w - 3 * p;
+            sb[p * SB + it.row * 3 + c] = ub[sweep_cell<AX>(it.row, x0, kk, a.nx, a.ny) * 3 + it.w];
+            sbk[p * SB + it.row * 3 + c] = ub[sweep_cell<AX>(it.row, x0, kn, a.nx, a.ny) * 3 + it.w];
+        }
+        for (RowIter it(tid, nt, 3); it.row < n; it.next())
+            sb[P * SB + it.row * 3 + it.w] = ub[sweep_cell<AX>(it.row, xn, kk, a.nx, a.ny) * 3 + it.w];
+        __syncthreads();
     }
-    __syncthreads();
-    mbar_wait_bounded(&bar, 0, a.err);
 
     const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
     using W = wide_t<R, EX>;
@@ -70,7 +103,7 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
     // ---- gather this thread's cells.  q and the cell-centred field are read
     // again from shared memory where they are needed later, which keeps them
     // out of the registers across the exchange phases.
-    const R* uq = su + (size_t)(lp * n + i0) * 5;
+    const R* uq = su + (size_t)lp * SU + (size_t)i0 * 5;
     auto load_q = [&](R (&q)[C][5]) {
         R qf[C * 5];
         lds_chunk<R, C * 5>(uq, qf);
@@ -78,23 +111,24 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
         for (int m = 0; m < C; m++)
 #pragma unroll
             for (int s = 0; s < 5; s++)
-                q[m][s] = qf[5 * m + s];
+                q[m][s] = qf[5 * m + sweep_u<AX>(s)];
     };
     auto load_f = [&](R (&f)[C][3]) {  // C/fluidx.c:71-81: b/2 + b(neighbour face)/2
         R bjf[C * 3], bpf[C * 3], bkf[C * 3];
-        const R* bj = sb + (size_t)(lp * n) * 3;
+        const R* bj = sb + (size_t)lp * SB;
         lds_chunk<R, C * 3>(bj + 3 * i0, bjf);
-        lds_chunk<R, C * 3>(sb + (size_t)((lp + 1) * n + i0) * 3, bpf);
-        lds_chunk<R, C * 3>(sbk + (size_t)(lp * n + i0) * 3, bkf);
+        lds_chunk<R, C * 3>(sb + (size_t)(lp + 1) * SB + (size_t)i0 * 3, bpf);
+        lds_chunk<R, C * 3>(sbk + (size_t)lp * SB + (size_t)i0 * 3, bkf);
         const int inext = (i0 + C == n) ? 0 : i0 + C;
-        const R b1next = bj[3 * inext];
+        constexpr int B0 = sweep_b<AX>(0), B1 = sweep_b<AX>(1), B2 = sweep_b<AX>(2);
+        const R b1next = bj[3 * inext + B0];
 #pragma unroll
         for (int m = 0; m < C; m++) {
-            const R h0 = R(0.5) * bjf[3 * m];
-            const R h0p = R(0.5) * ((m + 1 < C) ? bjf[3 * (m + 1)] : b1next);
+            const R h0 = R(0.5) * bjf[3 * m + B0];
+            const R h0p = R(0.5) * ((m + 1 < C) ? bjf[3 * (m + 1) + B0] : b1next);
             f[m][0] = h0 + h0p;
-            f[m][1] = R(0.5) * bjf[3 * m + 1] + bpf[3 * m + 1] / R(2);
-            f[m][2] = R(0.5) * bjf[3 * m + 2] + bkf[3 * m + 2] / R(2);
+            f[m][1] = R(0.5) * bjf[3 * m + B1] + bpf[3 * m + B1] / R(2);
+            f[m][2] = R(0.5) * bjf[3 * m + B2] + bkf[3 * m + B2] / R(2);
         }
     };
     R q[C][5], f[C][3];
@@ -235,15 +269,15 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
             for (int s = 0; s < 5; s++) {
                 q[m][s] = lin<R, EX>(R(1), q[m][s], mdt,
                                      lin<R, EX>(R(1), flux[m][s], R(-1), (m > 0) ? flux[m - 1][s] : fprev[s]));
-                of[5 * m + s] = q[m][s];
+                of[5 * m + sweep_u<AX>(s)] = q[m][s];
             }
         // own cells: no other thread reads them after the gather
-        sts_chunk<R, C * 5>(su + (size_t)(lp * n + i0) * 5, of);
+        sts_chunk<R, C * 5>(su + (size_t)lp * SU + (size_t)i0 * 5, of);
     }
 
-    // ---- optional calcfl epilogue on the new state (face b at (j,k))
-    if (a.cfl_part) {
-        const R* bj = sb + (size_t)(lp * n + i0) * 3;
+    // ---- optional calcfl epilogue on the new state (face b at (j,k)); x sweep only
+    if (AX == 0 && a.cfl_part) {
+        const R* bj = sb + (size_t)lp * SB + (size_t)i0 * 3;
         R m = R(0);
         int ln = -1;
 #pragma unroll
@@ -280,12 +314,22 @@ __global__ void __launch_bounds__(256) k_fluidx2(FluidxArgs a)
     }
 
     // ---- write the new pencils
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-        tma_store_1d(static_cast<R*>(a.u_out) + c0 * 5, su, 5u * np * sizeof(R));
-        tma_store_commit();
-        tma_store_wait_all();
+    if constexpr (AX == 0) {
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_1d(static_cast<R*>(a.u_out) + c0 * 5, su, 5u * np * sizeof(R));
+            tma_store_commit();
+            tma_store_wait_all();
+        }
+    } else {
+        __syncthreads();
+        const int x0 = blockIdx.x * P, kk = blockIdx.y;
+        R* uo = static_cast<R*>(a.u_out);
+        for (RowIter it(tid, blockDim.x, 5 * P); it.row < n; it.next()) {
+            const int p = it.w / 5, c = it.w - 5 * p;
+            uo[sweep_cell<AX>(it.row, x0, kk, a.nx, a.ny) * 5 + it.w] = su[p * SU + it.row * 5 + c];
+        }
     }
 }
 

@@ -44,6 +44,7 @@ struct FluidxArgs {
     void* cfl_part;       // optional fused calcfl epilogue: per-CTA partials (CflPart<R>)
     int* err;
     BoxStrides bs;
+    int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
 };
 
 struct AdvectArgs {
@@ -58,6 +59,7 @@ struct AdvectArgs {
     int* err;
     int K;                // planes per CTA along k for the marching kernel (nz % K == 0)
     BoxStrides bs;
+    int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
 };
 
 struct TransposeArgs {

@@ -23,6 +23,8 @@ struct KernelSet {
     size_t part_bytes; // sizeof(CflPart<R>)
     // number of CTAs (= CFL partials of the epilogue) of a fluidx launch
     int (*fluidx_parts)(int nx, int ny, int nz, int aligned);
+    // nonzero if the sweeps along y and z of the fused step have kernels for this grid
+    int (*fused_ok)(int nx, int ny, int nz);
 };
 
 const KernelSet* kernels_f32_fast();

@@ -14,6 +14,53 @@ constexpr int kSeamVals = 10;  // largest exchange (values per thread and round)
 
 // Contiguous chunk of NF values to/from shared memory; 128-bit accesses for
 // float when NF % 4 == 0 (the caller guarantees 16-byte alignment).
+// component of the untransposed state that the sweep along axis AX sees as
+// its component s: u (rho, m_d, m_j, m_k, E), b (b_d, b_j, b_k) with
+// (d, j, k) = (x, y, z), (y, x, z), (z, x, y)
+template <int AX>
+__host__ __device__ constexpr int sweep_u(int s)
+{
+    return AX == 0 ? s : (AX == 1 ? (s == 1 ? 2 : (s == 2 ? 1 : s)) : (s == 1 ? 3 : (s == 2 ? 1 : (s == 3 ? 2 : s))));
+}
+template <int AX>
+__host__ __device__ constexpr int sweep_b(int s)
+{
+    return AX == 0 ? s : (AX == 1 ? (s == 0 ? 1 : (s == 1 ? 0 : 2)) : (s == 0 ? 2 : (s == 1 ? 0 : 1)));
+}
+
+// linear cell of (position i along the sweep, x, plane k) for AX = 1 (k = z) and AX = 2 (k = y)
+template <int AX>
+__device__ __forceinline__ size_t sweep_cell(int i, int x, int k, int nx, int ny)
+{
+    return AX == 1 ? ((size_t)k * ny + i) * nx + x : ((size_t)i * ny + k) * nx + x;
+}
+
+// Walks the elements e = start, start + step, ... of a tile of rows of W
+// elements as (row, w) without a division per element.
+struct RowIter {
+    int row, w, drow, dw, W;
+    __device__ __forceinline__ RowIter(int start, int step, int W_) : W(W_)
+    {
+        row = start / W;
+        w = start - row * W;
+        drow = step / W;
+        dw = step - drow * W;
+    }
+    __device__ __forceinline__ void next()
+    {
+        row += drow;
+        w += dw;
+        if (w >= W) {
+            w -= W;
+            row++;
+        }
+    }
+};
+
+// padding (elements) of the pencil stride of tiles that the y/z sweeps fill
+// element by element: keeps the shared stores of a warp within 2-way conflicts
+constexpr int kSweepPad = 8;
+
 template <typename R, int NF>
 __device__ __forceinline__ void lds_chunk(const R* src, R (&dst)[NF])
 {

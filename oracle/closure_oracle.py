@@ -201,10 +201,11 @@ def targets(u_fine_next, b_fine_next, u_coarse, b_coarse, n, oscale, bscale):
 
 
 def apply_correction(u, b, out, n, oscale, bscale):
-    """u + oscale * out[:5]; b + bscale * curl_faces(out[5:])."""
+    """u + oscale * (out[:5] - box mean); b + bscale * curl_faces(out[5:])."""
     U, B = state_arrays(u, b, n)
     O = np.asarray(out, dtype=np.float64).reshape(n, n, n, 8)
-    U2 = U + O[..., :5] * np.asarray(oscale)
+    fl = O[..., :5] - O[..., :5].mean(axis=(0, 1, 2))
+    U2 = U + fl * np.asarray(oscale)
     B2 = B + bscale * curl_faces(O[..., 5:])
     return U2.reshape(-1), B2.reshape(-1)
 
