@@ -104,6 +104,19 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
                                           C.c_int]),
         "mhd_host_divb_max": (C.c_double, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
         "mhd_calcfl_noalloc": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
+        "mhd_write_check_value": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p]),
+        "mhd_read_init": (C.c_int, [C.c_char_p, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "mhd_checkpoint_save": (C.c_int, [C.c_char_p, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                          C.c_longlong]),
+        "mhd_checkpoint_info": (C.c_int, [C.c_char_p, _ip, _ip, _ip, _ip, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_longlong)]),
+        "mhd_checkpoint_load": (C.c_int, [C.c_char_p, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
+        "cuda_cfl": (None, [_vp, _vp, _ip, _ip, _ip, _vp, _vp, _ip, _ip, _ip, _fp]),
+        "cuda_fluidx": (None, [_vp, _vp, _ip, _ip, _ip, _vp, _ip, _ip, _ip]),
+        "cuda_advectbyzx": (None, [_vp, _vp, _ip, _ip, _ip, _vp, _vp, _ip, _ip, _ip]),
+        "cuda_transpose12": (None, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _ip, _ip, _ip]),
+        "cuda_transpose13": (None, [_vp, _vp, _vp, _vp, _ip, _ip, _ip, _ip, _ip, _ip]),
         "mhd_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, _ip, C.c_int]),
         "mhd_batch_destroy": (C.c_int, [_vp]),
         "mhd_batch_set_box": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_int]),
@@ -362,6 +375,49 @@ def init_turbulence(n, seed=0, rho0=1.0, p0=1.0, mach=0.5, bx0=0.3, dbrms=0.1, k
 
 def host_divb_max(b, nx, ny, nz) -> float:
     return float(lib().mhd_host_divb_max(_ptr(b), nx, ny, nz, int(b.dtype == np.float64)))
+
+
+# ------------------------------------------------------------ file formats
+
+def write_check_value(u, b, nx, ny, nz, directory: str = "") -> None:
+    """The reference's check_value dump (C/check_value.c): 8 text files, "%8.6e", i fastest."""
+    u = np.ascontiguousarray(u)
+    b = np.ascontiguousarray(b)
+    _check(lib().mhd_write_check_value(_ptr(u), _ptr(b), nx, ny, nz, int(u.dtype == np.float64),
+                                       str(directory).encode()), "mhd_write_check_value")
+
+
+def read_init(path, nx, ny, nz, fp64: bool = False):
+    """A state from a reference init file (C/init.c: 8 values per cell, i outer, k inner)."""
+    dt = np.float64 if fp64 else np.float32
+    n = nx * ny * nz
+    u = np.empty(5 * n, dtype=dt)
+    b = np.empty(3 * n, dtype=dt)
+    _check(lib().mhd_read_init(str(path).encode(), _ptr(u), _ptr(b), nx, ny, nz, int(fp64)), "mhd_read_init")
+    return u, b
+
+
+def checkpoint_save(path, u, b, nx, ny, nz, t: float = 0.0, step: int = 0) -> None:
+    u = np.ascontiguousarray(u)
+    b = np.ascontiguousarray(b)
+    _check(lib().mhd_checkpoint_save(str(path).encode(), _ptr(u), _ptr(b), nx, ny, nz, int(u.dtype == np.float64),
+                                     t, step), "mhd_checkpoint_save")
+
+
+def checkpoint_load(path):
+    """(u, b, (nx, ny, nz), t, step) of a checkpoint written by checkpoint_save."""
+    nx, ny, nz, f64 = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    t, step = C.c_double(), C.c_longlong()
+    p = str(path).encode()
+    _check(lib().mhd_checkpoint_info(p, C.byref(nx), C.byref(ny), C.byref(nz), C.byref(f64), C.byref(t),
+                                     C.byref(step)), "mhd_checkpoint_info")
+    dt = np.float64 if f64.value else np.float32
+    n = nx.value * ny.value * nz.value
+    u = np.empty(5 * n, dtype=dt)
+    b = np.empty(3 * n, dtype=dt)
+    _check(lib().mhd_checkpoint_load(p, _ptr(u), _ptr(b), nx.value, ny.value, nz.value, f64.value, C.byref(t),
+                                     C.byref(step)), "mhd_checkpoint_load")
+    return u, b, (nx.value, ny.value, nz.value), t.value, step.value
 
 
 # ------------------------------------------------------------ batched boxes

@@ -10,7 +10,8 @@ nvcc compiles the kernel sets for sm_103a only:
   * closure.cu       - the learned closure (BF16 tensor-core convolutions,
     loss, optimiser, filter and correction kernels);
 and gcc compiles the seeded initial conditions (mhd_init.c) with
--ffp-contract=off so they are identical on x86-64 and aarch64.  The
+-ffp-contract=off so they are identical on x86-64 and aarch64, and the
+file formats (mhd_io.c).  The
 translation units build in parallel; the result is
 heterogeneous_mhd_gb300/lib/libmhd_gb300.so.
 """
@@ -78,14 +79,17 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = OBJDIR / (src + ".o")
         if force or _stale(obj, [CSRC / src, *headers]):
             jobs.append(base + ["-c", str(CSRC / src), "-o", str(obj)])
-    init_obj = OBJDIR / "mhd_init.c.o"
-    if force or _stale(init_obj, [CSRC / "mhd_init.c", ROOT / "include" / "mhd_gb300.h"]):
-        jobs.append(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
-                     "-fvisibility=hidden", "-I", str(ROOT / "include"), "-c", str(CSRC / "mhd_init.c"),
-                     "-o", str(init_obj)])
+    c_objs = []
+    for csrc in ("mhd_init.c", "mhd_io.c"):  # host C: initial conditions, file formats
+        obj = OBJDIR / (csrc + ".o")
+        c_objs.append(obj)
+        if force or _stale(obj, [CSRC / csrc, *sorted((ROOT / "include").glob("*.h"))]):
+            jobs.append(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
+                         "-fvisibility=hidden", "-I", str(ROOT / "include"), "-c", str(CSRC / csrc),
+                         "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=4) as ex:
         list(ex.map(_run, jobs))
-    objs = [OBJDIR / (u[0] + ".o") for u in units] + [init_obj]
+    objs = [OBJDIR / (u[0] + ".o") for u in units] + c_objs
     lib = lib_path()
     if force or jobs or _stale(lib, objs):
         _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fopenmp",

@@ -66,6 +66,8 @@ def _sig():
         "mhd_cl_apply": (i, [vp, vp, vp, i, vp, f, vp, vp, vp, vp, f, vp, vp]),
         "mhd_cl_adamw": (i, [vp, vp, vp, vp, ll, i, f, f, f, f, f, vp]),
         "mhd_cl_pack": (i, [vp, i, i, i, i, i, vp, vp, vp]),
+        "mhd_cl_use_tcgen05": (i, [i]),
+        "mhd_cl_device_errors": (i, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -260,6 +260,226 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ x, const 
     }
 }
 
+// ------------------------------------------------------------ tcgen05 path
+//
+// The same 3^3 convolution on the 5th-generation tensor cores.  A persistent
+// CTA (8 warps) takes tiles of 16 (x) x 8 (y) x 2 (z) voxels: two M = 128
+// blocks (one per plane, rows m = 8 x + y).  Its halo tile (18 x 10 x 4
+// voxels) sits in shared memory chunk-major, [channel chunk of 8][z'][x'][y']
+// x 16 B, so for every plane and tap (dk, dj, di) the A operand is one
+// K-major no-swizzle descriptor: 8-row core matrices are 8 consecutive y'
+// (128 B), the 16 row groups (x) are 160 B apart (SBO) and the two 8-channel
+// chunks of a K-step one chunk apart (LBO); plane and tap only move the start
+// address, a compile-time offset.  The weights ([K chunk][cout] x 16 B) stay
+// resident.  One thread issues the 2 x 27 x CIN/16 MMAs (M = 128, N = COUT,
+// K = 16, BF16 in, FP32 accumulate) into one of two TMEM buffers and commits
+// them to that buffer's mbarrier; meanwhile all warps run the epilogue of the
+// previous tile from the other buffer (tcgen05.ld 32x32b: warp w reads plane
+// w / 4, lanes 32 (w % 4)..) and the next tile's halo arrives by cp.async
+// into the other shared buffer.  Waits are bounded: on timeout the kernel
+// records DEVERR_TIMEOUT, stops and frees its TMEM.
+
+constexpr int TCX = 16, TCY = 8, TCZ = 2;                    // tile
+constexpr int HX = TCX + 2, HY = TCY + 2, HZ = TCZ + 2;      // halo tile
+constexpr int HV = HX * HY * HZ;                             // 720 voxels
+constexpr uint32_t kChunkBytes = HV * 16;                    // one 8-channel chunk of the halo
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, int acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+template <int CIN>
+__device__ __forceinline__ void tc_load_halo(unsigned char* dst, const bf16* src, int box, int z0, int y0, int x0,
+                                             int n)
+{
+    constexpr int CH = CIN / 8;
+    const size_t box0 = (size_t)box * n * n * n;
+    // consecutive threads: chunks of one voxel, then x (contiguous rows in HBM)
+    for (int e = threadIdx.x; e < HV * CH; e += blockDim.x) {
+        const int c = e % CH, r = e / CH;
+        const int xp = r % HX, r2 = r / HX, yp = r2 % HY, zp = r2 / HY;
+        const int gx = wrap(x0 + xp - 1, n), gy = wrap(y0 + yp - 1, n), gz = wrap(z0 + zp - 1, n);
+        const bf16* s = src + (box0 + ((size_t)gz * n + gy) * n + gx) * CIN + c * 8;
+        cp_async16(dst + c * kChunkBytes + ((zp * HX + xp) * HY + yp) * 16, s);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// all MMAs of one tile: plane P, tap T, K-step KS; offsets are compile-time
+template <int CIN, int COUT>
+__device__ __forceinline__ void tc_issue_tile(uint32_t tmem, uint64_t a_desc0, uint64_t b_desc0, uint32_t idesc)
+{
+    constexpr int CH = CIN / 8;
+#pragma unroll
+    for (int p = 0; p < TCZ; p++)
+#pragma unroll
+        for (int tap = 0; tap < 27; tap++)
+#pragma unroll
+            for (int ks = 0; ks < CIN / 16; ks++) {
+                const int dk = tap / 9, dj = (tap / 3) % 3, di = tap % 3;
+                const uint32_t aoff = (((dk + p) * HX + di) * HY + dj) * 16 + 2 * ks * kChunkBytes;
+                const uint32_t boff = (uint32_t)(tap * CH + 2 * ks) * COUT * 16;
+                umma_f16(tmem + 32 * p, a_desc0 + (aoff >> 4), b_desc0 + (boff >> 4), idesc, tap | ks);
+            }
+}
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(256, 1) k_conv_tc(const bf16* __restrict__ x, const bf16* __restrict__ w,
+                                                     const float* __restrict__ bias, void* __restrict__ y,
+                                                     bf16* __restrict__ zsave, const bf16* __restrict__ zprev, int n,
+                                                     long long ntiles, int* err)
+{
+    static_assert(COUT == 32, "one tile's accumulators are 2 x 32 TMEM columns");
+    constexpr int CH = CIN / 8;
+    constexpr int KC = 27 * CH;                  // K chunks of the weights
+    constexpr uint32_t ABYTES = CH * kChunkBytes;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char* sW = sm + 2 * ABYTES;         // [KC][COUT][16 B]
+    __shared__ __align__(8) uint64_t mma_bar[2];
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // weights: global [COUT][27][CIN] bf16 -> [K chunk][cout] x 16 B
+    for (int e = tid; e < KC * COUT; e += blockDim.x) {
+        const int co = e % COUT, kc = e / COUT;
+        cp_async16(sW + ((size_t)kc * COUT + co) * 16, w + (size_t)co * 27 * CIN + kc * 8);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    if (tid == 0) {
+        for (int b = 0; b < 2; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mhd::smem_u32(&mma_bar[b])));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+                         mhd::smem_u32(&tmem_base)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | (8u << 24);
+    const uint64_t a_desc[2] = {umma_desc(mhd::smem_u32(sm), kChunkBytes, HY * 16),
+                                umma_desc(mhd::smem_u32(sm + ABYTES), kChunkBytes, HY * 16)};
+    const uint64_t b_desc = umma_desc(mhd::smem_u32(sW), COUT * 16, 128);
+
+    const int tx = n / TCX, ty = n / TCY, tz = n / TCZ;
+    auto coords = [&](long long t, int& box, int& z0, int& y0, int& x0) {
+        x0 = (int)(t % tx) * TCX;
+        t /= tx;
+        y0 = (int)(t % ty) * TCY;
+        t /= ty;
+        z0 = (int)(t % tz) * TCZ;
+        box = (int)(t / tz);
+    };
+    if ((long long)blockIdx.x < ntiles) {
+        int b_, z_, y_, x_;
+        coords(blockIdx.x, b_, z_, y_, x_);
+        tc_load_halo<CIN>(sm, x, b_, z_, y_, x_, n);
+    }
+    int pbox = 0, pz = 0, py = 0, px = 0;  // the previous tile (its epilogue runs this iteration)
+    for (long long it = 0;; it++) {
+        const long long tile = blockIdx.x + it * gridDim.x;
+        const bool cur = tile < ntiles;
+        const int ab = (int)(it & 1);
+        // (1) the previous tile's MMAs: its A buffer is refilled and its TMEM read below
+        if (it > 0) {
+            const int pb = (int)((it - 1) & 1);
+            const bool ok = mhd::mbar_wait_bounded(&mma_bar[pb], (uint32_t)(((it - 1) >> 1) & 1), err);
+            if (__syncthreads_or(!ok))
+                break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        // (2) prefetch the next tile into the other A buffer; (3) wait for this tile's halo
+        int box = 0, z0 = 0, y0 = 0, x0 = 0;
+        if (cur) {
+            coords(tile, box, z0, y0, x0);
+            const long long next = tile + gridDim.x;
+            if (next < ntiles) {
+                int b_, z_, y_, x_;
+                coords(next, b_, z_, y_, x_);
+                tc_load_halo<CIN>(sm + (ab ^ 1) * ABYTES, x, b_, z_, y_, x_, n);
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+            } else {
+                asm volatile("cp.async.wait_group 0;" ::: "memory");
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async writes -> tensor core
+        }
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // (4) this tile's MMAs into TMEM columns 64 ab .. 64 ab + 63
+        if (cur && tid == 0) {
+            tc_issue_tile<CIN, COUT>(tmem + 64 * ab, a_desc[ab], b_desc, idesc);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             mhd::smem_u32(&mma_bar[ab]))
+                         : "memory");
+        }
+        // (5) epilogue of the previous tile
+        if (it > 0) {
+            const int pb = (int)((it - 1) & 1), pl = warp >> 2, q = warp & 3;
+            uint32_t r[32];
+            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + 64 * pb + 32 * pl;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                         "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                           "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                           "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int m = q * 32 + lane, vx = m >> 3, vy = m & 7;
+            const size_t v = (((size_t)pbox * n + pz + pl) * n + (py + vy)) * n + (px + vx);
+            __align__(16) bf16 o1[COUT];
+            __align__(16) bf16 o2[COUT];
+#pragma unroll
+            for (int c = 0; c < COUT; c += 2) {
+                const float v0 = __uint_as_float(r[c]), v1 = __uint_as_float(r[c + 1]);
+                if constexpr (EPI == EPI_GELU) {
+                    const __nv_bfloat162 zz = __floats2bfloat162_rn(v0 + bias[c], v1 + bias[c + 1]);
+                    const float2 zf = __bfloat1622float2(zz);
+                    *reinterpret_cast<__nv_bfloat162*>(o2 + c) = zz;
+                    *reinterpret_cast<__nv_bfloat162*>(o1 + c) = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
+                } else {
+                    const float2 zp =
+                        __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zprev + v * COUT + c));
+                    *reinterpret_cast<__nv_bfloat162*>(o1 + c) =
+                        __floats2bfloat162_rn(v0 * gelu_grad(zp.x), v1 * gelu_grad(zp.y));
+                }
+            }
+            uint4* yo = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + v * COUT);
+#pragma unroll
+            for (int k = 0; k < COUT / 8; k++)
+                yo[k] = reinterpret_cast<const uint4*>(o1)[k];
+            if constexpr (EPI == EPI_GELU) {
+                uint4* zo = reinterpret_cast<uint4*>(zsave + v * COUT);
+#pragma unroll
+                for (int k = 0; k < COUT / 8; k++)
+                    zo[k] = reinterpret_cast<const uint4*>(o2)[k];
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (!cur)
+            break;
+        pbox = box, pz = z0, py = y0, px = x0;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+}
+
 // dW(co, tap, ci) = sum_v dz(v, co) a(v + off(tap), ci).  Warp w owns the taps
 // t == w mod WT and the k-steps (16 voxels) s == w / WT mod WK.  Each warp
 // writes its FP32 partial sums to part[cta][w / WT][tap][co][ci].
@@ -782,6 +1002,34 @@ int launch_conv(const void* x, const void* w, const float* bias, void* y, void* 
     return st(cudaGetLastError());
 }
 
+int* g_tc_err = nullptr;  // device error word of the tcgen05 kernels
+bool g_tc_disabled = false;
+
+template <int CIN, int COUT, int EPI>
+int launch_conv_tc(const void* x, const void* w, const float* bias, void* y, void* zsave, const void* zprev, int nb,
+                   int n, cudaStream_t s)
+{
+    const size_t smem = 2 * (size_t)(CIN / 8) * kChunkBytes + (size_t)27 * (CIN / 8) * COUT * 16;  // A x 2, W
+    static bool attr = false;
+    if (!attr) {
+        if (set_smem(k_conv_tc<CIN, COUT, EPI>, smem) != cudaSuccess)
+            return MHD_ERR_CUDA;
+        attr = true;
+    }
+    if (!g_tc_err && cudaMalloc(&g_tc_err, sizeof(int)) == cudaSuccess)
+        cudaMemset(g_tc_err, 0, sizeof(int));
+    if (!g_tc_err)
+        return MHD_ERR_NOMEM;
+    const long long ntiles = (long long)nb * (n / TCX) * (n / TCY) * (n / TCZ);
+    const long long grid = ntiles < (long long)sms() ? ntiles : (long long)sms();
+    k_conv_tc<CIN, COUT, EPI><<<(unsigned)grid, 256, smem, s>>>(
+        static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias, y, static_cast<bf16*>(zsave),
+        static_cast<const bf16*>(zprev), n, ntiles, g_tc_err);
+    return st(cudaGetLastError());
+}
+
+bool use_tc(int n) { return !g_tc_disabled && n % TCX == 0 && n % TCY == 0 && n % TCZ == 0; }
+
 template <int CIN, int COUTP, int KS>
 size_t wgrad_parts(int nb, int n)
 {
@@ -837,17 +1085,47 @@ extern "C" MHD_API int mhd_cl_conv(int kind, const void* x, const void* w, const
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (kind) {
     case MHD_CL_FWD_IN:
-        return (bias && zsave) ? launch_conv<16, 32, 3, EPI_GELU>(x, w, bias, y, zsave, nullptr, nb, n, s) : MHD_ERR_ARG;
+        if (!bias || !zsave)
+            return MHD_ERR_ARG;
+        return use_tc(n) ? launch_conv_tc<16, 32, EPI_GELU>(x, w, bias, y, zsave, nullptr, nb, n, s)
+                         : launch_conv<16, 32, 3, EPI_GELU>(x, w, bias, y, zsave, nullptr, nb, n, s);
     case MHD_CL_FWD_HID:
-        return (bias && zsave) ? launch_conv<32, 32, 3, EPI_GELU>(x, w, bias, y, zsave, nullptr, nb, n, s) : MHD_ERR_ARG;
+        if (!bias || !zsave)
+            return MHD_ERR_ARG;
+        return use_tc(n) ? launch_conv_tc<32, 32, EPI_GELU>(x, w, bias, y, zsave, nullptr, nb, n, s)
+                         : launch_conv<32, 32, 3, EPI_GELU>(x, w, bias, y, zsave, nullptr, nb, n, s);
     case MHD_CL_FWD_HEAD:
         return bias ? launch_conv<32, 8, 1, EPI_LINEAR_F32>(x, w, bias, y, nullptr, nullptr, nb, n, s) : MHD_ERR_ARG;
     case MHD_CL_DGRAD_HEAD:
         return zprev ? launch_conv<16, 32, 1, EPI_DGRAD>(x, w, nullptr, y, nullptr, zprev, nb, n, s) : MHD_ERR_ARG;
     case MHD_CL_DGRAD_HID:
-        return zprev ? launch_conv<32, 32, 3, EPI_DGRAD>(x, w, nullptr, y, nullptr, zprev, nb, n, s) : MHD_ERR_ARG;
+        if (!zprev)
+            return MHD_ERR_ARG;
+        return use_tc(n) ? launch_conv_tc<32, 32, EPI_DGRAD>(x, w, nullptr, y, nullptr, zprev, nb, n, s)
+                         : launch_conv<32, 32, 3, EPI_DGRAD>(x, w, nullptr, y, nullptr, zprev, nb, n, s);
     }
     return MHD_ERR_ARG;
+}
+
+// 1: the 3^3 convolutions of edges that are multiples of 16 run on tcgen05 (the default); 0: the
+// mma.sync kernels everywhere.  Returns the previous setting.
+extern "C" MHD_API int mhd_cl_use_tcgen05(int enable)
+{
+    const int prev = g_tc_disabled ? 0 : 1;
+    g_tc_disabled = (enable == 0);
+    return prev;
+}
+
+// Error bits of the tcgen05 kernels' bounded waits (DEVERR_TIMEOUT), cleared by the read.
+extern "C" MHD_API int mhd_cl_device_errors(void)
+{
+    if (!g_tc_err)
+        return 0;
+    int h = 0;
+    if (cudaMemcpy(&h, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return -1;
+    cudaMemset(g_tc_err, 0, sizeof(int));
+    return h;
 }
 
 extern "C" MHD_API long long mhd_cl_wgrad_scratch(int kind, int nb, int n)

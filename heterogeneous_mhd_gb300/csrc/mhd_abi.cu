@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/mhd_gb300.h"
+#include "../../include/mhd_cuda_compat.h"
 #include "mhd_launch.h"
 
 using namespace mhd;
@@ -1142,4 +1143,112 @@ extern "C" MHD_API float calcfl(float* u, float* b, int* nx, int* ny, int* nz)
     int s = calcfl_sync(c, args[0].dev, args[1].dev, *nx, *ny, *nz, &inv);
     set_err(s);
     return (float)inv;
+}
+
+// ------------------------------------------------- CUDA-side compatibility names
+//
+// The reference's CUDA host code (Cuda/cuda_subroutine.h:4-12) calls these
+// five names with device arrays, device copies of the dimensions (ignored
+// here) and host copies (used).  They run this library's kernels with the
+// C path's arithmetic (Cuda/ itself diverges from C/), on the drop-in
+// context, and return after the work is done like the reference's
+// cudaThreadSynchronize.
+
+static bool host_dims_ok(const int* nx, const int* ny, const int* nz)
+{
+    return nx && ny && nz && *nx > 0 && *ny > 0 && *nz > 0;
+}
+
+// dt <- 1/max speed (Cuda/cuda_cfl.cu:14-45): *h_dt on the host and a copy in dt (device)
+extern "C" MHD_API void cuda_cfl(float* u, float* b, int* nx, int* ny, int* nz, float* dt, float* c_scratch,
+                                 int* h_nx, int* h_ny, int* h_nz, float* h_dt)
+{
+    (void)nx, (void)ny, (void)nz, (void)c_scratch;
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !b || !dt || !h_dt || !host_dims_ok(h_nx, h_ny, h_nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    double inv = NAN;
+    if (set_err(calcfl_sync(c, u, b, *h_nx, *h_ny, *h_nz, &inv)) != MHD_OK)
+        return;
+    *h_dt = (float)inv;
+    set_err(cudaMemcpy(dt, h_dt, sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA);
+}
+
+// u <- fluidx(u, b) in place, dt read on the device (Cuda/cuda_fluidx.cu:12-23)
+extern "C" MHD_API void cuda_fluidx(float* u, float* b, int* nx, int* ny, int* nz, float* dt, int* h_nx, int* h_ny,
+                                    int* h_nz)
+{
+    (void)nx, (void)ny, (void)nz;
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !b || !dt || !host_dims_ok(h_nx, h_ny, h_nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    // in place is safe: a CTA reads only its own u pencils (and b)
+    if (set_err(op_fluidx(c, u, u, b, *h_nx, *h_ny, *h_nz, 0.0, dt, nullptr)) != MHD_OK)
+        return;
+    set_err(cudaStreamSynchronize(c->stream) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA);
+}
+
+// b <- advectbyzx(u, b) in place (Cuda/cuda_advectbyzx.cu); `temp` (the reference's EMF
+// scratch) is not needed
+extern "C" MHD_API void cuda_advectbyzx(float* u, float* b, int* nx, int* ny, int* nz, float* dt, float* temp,
+                                        int* h_nx, int* h_ny, int* h_nz)
+{
+    (void)nx, (void)ny, (void)nz, (void)temp;
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!u || !b || !dt || !host_dims_ok(h_nx, h_ny, h_nz)) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    const size_t bytes = (size_t)(*h_nx) * (*h_ny) * (*h_nz) * 12;
+    // neighbouring rows of b are read while b is written: advect from a private copy
+    if (set_err(c->alias[1].ensure(bytes)) != MHD_OK || set_err(op_copy(c, b, c->alias[1].p, bytes)) != MHD_OK)
+        return;
+    if (set_err(op_advect(c, b, c->alias[1].p, u, c->alias[1].p, *h_nx, *h_ny, *h_nz, 0.0, dt)) != MHD_OK)
+        return;
+    set_err(cudaStreamSynchronize(c->stream) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA);
+}
+
+static void cuda_transpose(int axis, float* ut, float* bt, float* u, float* b, const int* h_nx, const int* h_ny,
+                           const int* h_nz)
+{
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!ut || !bt || !u || !b || !host_dims_ok(h_nx, h_ny, h_nz) || ut == u || bt == b) {
+        set_err(MHD_ERR_ARG);
+        return;
+    }
+    mhd_ctx* c;
+    if (set_err(dropin_ctx(&c)) != MHD_OK)
+        return;
+    if (set_err(op_transpose(c, axis, ut, bt, u, b, *h_nx, *h_ny, *h_nz)) != MHD_OK)
+        return;
+    set_err(cudaStreamSynchronize(c->stream) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA);
+}
+
+// (ut, bt) <- transpose12(u, b) (Cuda/cuda_transpose12.cu)
+extern "C" MHD_API void cuda_transpose12(float* ut, float* bt, float* u, float* b, int* nx, int* ny, int* nz,
+                                         int* h_nx, int* h_ny, int* h_nz)
+{
+    (void)nx, (void)ny, (void)nz;
+    cuda_transpose(1, ut, bt, u, b, h_nx, h_ny, h_nz);
+}
+
+// (ut, bt) <- transpose13(u, b), nx == nz (Cuda/cuda_transpose13.cu)
+extern "C" MHD_API void cuda_transpose13(float* ut, float* bt, float* u, float* b, int* nx, int* ny, int* nz,
+                                         int* h_nx, int* h_ny, int* h_nz)
+{
+    (void)nx, (void)ny, (void)nz;
+    cuda_transpose(2, ut, bt, u, b, h_nx, h_ny, h_nz);
 }

@@ -105,22 +105,14 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
                 }
             }
         } else {
-            // rows of u at x0-1..x0+J and of b at x0..x0+J, position i of plane pp,
-            // word by word over consecutive threads
-            for (RowIter it(tid, blockDim.x, 5 * (J + 2)); it.row < n; it.next()) {
-                const int pj = it.w / 5, c = it.w - 5 * pj;
-                int x = j0 - 1 + pj;
-                x = (x < 0) ? x + ny : (x >= ny ? x - ny : x);
-                cp_async4(U + s * uslab + (size_t)pj * UROW + it.row * 5 + c,
-                          uu + sweep_cell<AX>(it.row, x, pp, a.nx, a.ny) * 5 + c);
-            }
-            for (RowIter it(tid, blockDim.x, 3 * (J + 1)); it.row < n; it.next()) {
-                const int pj = it.w / 3, c = it.w - 3 * pj;
-                int x = j0 + pj;
-                x = (x >= ny) ? x - ny : x;
-                cp_async4(B + s * bslab + (size_t)pj * BROW + it.row * 3 + c,
-                          ub + sweep_cell<AX>(it.row, x, pp, a.nx, a.ny) * 3 + c);
-            }
+            // rows of u at x0-1..x0+J and of b at x0..x0+J (x periodic) of plane pp
+            const size_t rs = (AX == 1) ? (size_t)a.nx : (size_t)a.nx * a.ny;
+            const float* u0 = uu + sweep_cell<AX>(0, 0, pp, a.nx, a.ny) * 5;
+            const float* b0 = ub + sweep_cell<AX>(0, 0, pp, a.nx, a.ny) * 3;
+            auto ucol = [&](int p) { int x = j0 - 1 + p; return (x < 0) ? x + ny : (x >= ny ? x - ny : x); };
+            auto bcol = [&](int p) { int x = j0 + p; return (x >= ny) ? x - ny : x; };
+            gather_tile<5>(U + s * uslab, UROW, u0, rs * 5, J + 2, n, ucol, tid, blockDim.x);
+            gather_tile<3>(B + s * bslab, BROW, b0, rs * 3, J + 1, n, bcol, tid, blockDim.x);
             cp_async_commit();
         }
     };
@@ -278,11 +270,9 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         }
         if constexpr (AX != 0) {  // the J combined pencils back as rows of consecutive x
             __syncthreads();
-            const int pk_ = k % nz;
-            for (RowIter it(tid, blockDim.x, 3 * J); it.row < n; it.next()) {
-                const int p = it.w / 3, c = it.w - 3 * p;
-                bo[sweep_cell<AX>(it.row, j0, pk_, a.nx, a.ny) * 3 + it.w] = SO[(size_t)p * BROW + it.row * 3 + c];
-            }
+            const size_t rs = (AX == 1) ? (size_t)a.nx : (size_t)a.nx * a.ny;
+            scatter_tile<3>(bo + sweep_cell<AX>(0, j0, k % nz, a.nx, a.ny) * 3, rs * 3, SO, BROW, J, n, tid,
+                            blockDim.x);
         }
         // the B rows' advected b(3) of plane k+1, for the next step
         if (brow) {

@@ -83,17 +83,22 @@ __global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
         const int kn = (kk + 1 == nk) ? 0 : kk + 1;
         const int xn = (x0 + P == a.nx) ? 0 : x0 + P;
         const int nt = blockDim.x;
-        for (RowIter it(tid, nt, 5 * P); it.row < n; it.next()) {
-            const int p = it.w / 5, c = it.w - 5 * p;
-            su[p * SU + it.row * 5 + c] = uu[sweep_cell<AX>(it.row, x0, kk, a.nx, a.ny) * 5 + it.w];
+        // rows along the sweep are rstride cells apart; 4-byte cp.async, all in flight at once
+        const size_t rs = (AX == 1) ? (size_t)a.nx : (size_t)a.nx * a.ny;
+        if constexpr (sizeof(R) == 4) {
+            const float* u0 = reinterpret_cast<const float*>(uu) + sweep_cell<AX>(0, x0, kk, a.nx, a.ny) * 5;
+            const float* b0 = reinterpret_cast<const float*>(ub) + sweep_cell<AX>(0, x0, kk, a.nx, a.ny) * 3;
+            const float* bk0 = reinterpret_cast<const float*>(ub) + sweep_cell<AX>(0, x0, kn, a.nx, a.ny) * 3;
+            const float* bn0 = reinterpret_cast<const float*>(ub) + sweep_cell<AX>(0, xn, kk, a.nx, a.ny) * 3;
+            auto same = [](int p) { return p; };
+            auto zero = [](int) { return 0; };
+            gather_tile<5>(reinterpret_cast<float*>(su), SU, u0, rs * 5, P, n, same, tid, nt);
+            gather_tile<3>(reinterpret_cast<float*>(sb), SB, b0, rs * 3, P, n, same, tid, nt);
+            gather_tile<3>(reinterpret_cast<float*>(sbk), SB, bk0, rs * 3, P, n, same, tid, nt);
+            gather_tile<3>(reinterpret_cast<float*>(sb) + P * SB, SB, bn0, rs * 3, 1, n, zero, tid, nt);
+            cp_async_commit();
+            cp_async_wait<0>();
         }
-        for (RowIter it(tid, nt, 3 * P); it.row < n; it.next()) {
-            const int p = it.w / 3, c = it.w - 3 * p;
-            sb[p * SB + it.row * 3 + c] = ub[sweep_cell<AX>(it.row, x0, kk, a.nx, a.ny) * 3 + it.w];
-            sbk[p * SB + it.row * 3 + c] = ub[sweep_cell<AX>(it.row, x0, kn, a.nx, a.ny) * 3 + it.w];
-        }
-        for (RowIter it(tid, nt, 3); it.row < n; it.next())
-            sb[P * SB + it.row * 3 + it.w] = ub[sweep_cell<AX>(it.row, xn, kk, a.nx, a.ny) * 3 + it.w];
         __syncthreads();
     }
 
@@ -324,11 +329,11 @@ __global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
         }
     } else {
         __syncthreads();
-        const int x0 = blockIdx.x * P, kk = blockIdx.y;
-        R* uo = static_cast<R*>(a.u_out);
-        for (RowIter it(tid, blockDim.x, 5 * P); it.row < n; it.next()) {
-            const int p = it.w / 5, c = it.w - 5 * p;
-            uo[sweep_cell<AX>(it.row, x0, kk, a.nx, a.ny) * 5 + it.w] = su[p * SU + it.row * 5 + c];
+        if constexpr (sizeof(R) == 4) {
+            const int x0 = blockIdx.x * P, kk = blockIdx.y;
+            const size_t rs = (AX == 1) ? (size_t)a.nx : (size_t)a.nx * a.ny;
+            float* uo = static_cast<float*>(a.u_out) + sweep_cell<AX>(0, x0, kk, a.nx, a.ny) * 5;
+            scatter_tile<5>(uo, rs * 5, reinterpret_cast<const float*>(su), SU, P, n, tid, blockDim.x);
         }
     }
 }

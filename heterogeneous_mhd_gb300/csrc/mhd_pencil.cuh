@@ -57,6 +57,61 @@ struct RowIter {
     }
 };
 
+// Gather an n-row tile into pencil-major shared memory: row r of the tile is
+// W = pencils x NC consecutive words at src_row0 + r * rstride (pencil p of
+// the row starting at word col(p) * NC of it), and word (p, c) of row r goes
+// to dst[p * PS + r * NC + c].  Each thread owns one fixed column w of the
+// tile and walks the rows, so an element costs one 4-byte cp.async and two
+// pointer increments; consecutive threads read consecutive words.
+template <int NC, typename Col>
+__device__ __forceinline__ void gather_tile(float* dst, int PS, const float* src_row0, size_t rstride, int pencils,
+                                            int n, Col col, int tid, int nt)
+{
+    const int W = pencils * NC, rpp = nt / W;
+    if (rpp == 0) {  // fewer threads than columns: a thread walks several columns
+        for (int w = tid; w < W; w += nt) {
+            const int p = w / NC, c = w - p * NC;
+            for (int r = 0; r < n; r++)
+                cp_async4(dst + p * PS + r * NC + c, src_row0 + (size_t)col(p) * NC + c + (size_t)r * rstride);
+        }
+        return;
+    }
+    if (tid >= rpp * W)
+        return;
+    const int w = tid % W, r0 = tid / W;
+    const int p = w / NC, c = w - p * NC;
+    float* d = dst + p * PS + r0 * NC + c;
+    const float* s = src_row0 + (size_t)col(p) * NC + c + (size_t)r0 * rstride;
+    const size_t sstep = (size_t)rpp * rstride;
+    for (int r = r0; r < n; r += rpp, d += rpp * NC, s += sstep)
+        cp_async4(d, s);
+}
+
+// The inverse: row r of a pencil-major shared tile back to its global row.
+template <int NC>
+__device__ __forceinline__ void scatter_tile(float* dst_row0, size_t rstride, const float* src, int PS, int pencils,
+                                             int n, int tid, int nt)
+{
+    const int W = pencils * NC, rpp = nt / W;
+    if (rpp == 0) {
+        for (int w = tid; w < W; w += nt) {
+            const int p = w / NC, c = w - p * NC;
+            for (int r = 0; r < n; r++)
+                dst_row0[w + (size_t)r * rstride] = src[p * PS + r * NC + c];
+        }
+        return;
+    }
+    if (tid >= rpp * W)
+        return;
+    const int w = tid % W, r0 = tid / W;
+    const int p = w / NC, c = w - p * NC;
+    const float* s = src + p * PS + r0 * NC + c;
+    float* d = dst_row0 + w + (size_t)r0 * rstride;
+    const size_t dstep = (size_t)rpp * rstride;
+    for (int r = r0; r < n; r += rpp, s += rpp * NC, d += dstep)
+        *d = *s;
+}
+
 // padding (elements) of the pencil stride of tiles that the y/z sweeps fill
 // element by element: keeps the shared stores of a warp within 2-way conflicts
 constexpr int kSweepPad = 8;

@@ -233,3 +233,44 @@ def test_training_fits_a_teacher(clos, cuda):
         if it % 50 == 0 or it == 299:
             losses.append(student.loss_value())
     assert losses[-1] < 0.1 * losses[0], losses
+
+
+@pytest.mark.parametrize("kind", ["in", "hid", "dgrad"])
+def test_tcgen05_conv_matches_mma_sync(kind, clos, cuda):
+    """The tcgen05 kernel (n a multiple of 16) against the mma.sync kernel on the same operands."""
+    torch = cuda
+    L = clos.cl()
+    rng = np.random.default_rng(8)
+    nb, n = 2, 32
+    cin = 16 if kind == "in" else 32
+    s = clos.stream_ptr()
+    w = rng.normal(size=(32, 27, 8 if kind == "in" else 32)) * 0.05
+    wf = torch.empty(32 * 27 * cin, dtype=torch.bfloat16, device="cuda")
+    wd = torch.empty(32 * 27 * cin, dtype=torch.bfloat16, device="cuda")
+    assert L.mhd_cl_pack(to_f32(torch, w).data_ptr(), 32, w.shape[2], 27, 32, cin, wf.data_ptr(),
+                         wd.data_ptr() if kind != "in" else None, s) == 0
+    x = rng.normal(size=(nb, n, n, n, cin))
+    if kind == "in":
+        x[..., 8:] = 0
+    xd = to_bf16(torch, x)
+    bd = to_f32(torch, rng.normal(size=32) * 0.1)
+    zp = to_bf16(torch, rng.normal(size=(nb, n, n, n, 32)))
+    outs = []
+    for tc in (1, 0):
+        L.mhd_cl_use_tcgen05(tc)
+        y = torch.empty(nb * n ** 3 * 32, dtype=torch.bfloat16, device="cuda")
+        z = torch.zeros_like(y)
+        if kind == "dgrad":
+            st = L.mhd_cl_conv(clos.DGRAD_HID, xd.data_ptr(), wd.data_ptr(), None, y.data_ptr(), None,
+                               zp.data_ptr(), nb, n, s)
+        else:
+            st = L.mhd_cl_conv(clos.FWD_IN if kind == "in" else clos.FWD_HID, xd.data_ptr(), wf.data_ptr(),
+                               bd.data_ptr(), y.data_ptr(), z.data_ptr(), None, nb, n, s)
+        assert st == 0
+        torch.cuda.synchronize()
+        outs.append((bf_np(y), bf_np(z)))
+    L.mhd_cl_use_tcgen05(1)
+    assert L.mhd_cl_device_errors() == 0
+    assert rel(outs[0][0], outs[1][0]) < 8e-3  # FP32 accumulation in two orders, one BF16 rounding
+    if kind != "dgrad":
+        assert rel(outs[0][1], outs[1][1]) < 8e-3
