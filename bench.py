@@ -215,23 +215,27 @@ def fp64_error_leg(mhd, n: int, steps: int):
 CLOSURE_WEIGHTS = ROOT / "heterogeneous_mhd_gb300" / "closure_weights.npz"
 
 
-def closure_leg(seeds=(1000,), fine=256, factor=4, crossings=2.0):
-    """The closure at matched error: a held-out vortex seed run to `crossings`
-    turbulent crossing times at fine^3 (plain) and at (fine/factor)^3 (plain,
-    and plain + the trained closure after every step), compared after
+def closure_leg(seeds=(1000,), fine=256, factor=4, horizons=(0.5, 1.0, 2.0)):
+    """The closure at matched error: a held-out vortex seed run to each horizon
+    (turbulent crossing times) at fine^3 (plain) and at (fine/factor)^3
+    (plain, and plain + the trained closure after every step), compared after
     filtering the fine run; GPU time of the fine run over the closure run."""
     if not CLOSURE_WEIGHTS.exists():
         return {"unavailable": "no trained closure weights in the package"}
     from heterogeneous_mhd_gb300 import closure, closure_train
 
     net = closure.ClosureNet.load(CLOSURE_WEIGHTS)
-    rep = closure_train.evaluate(net, list(seeds), fine, factor, crossings, log=None)
-    out = {"workload": f"vortex seeds {list(seeds)}, {fine}^3 plain vs {fine // factor}^3 plain and "
-                       f"{fine // factor}^3 + closure, {crossings} crossing times", **rep["summary"]}
+    rep = closure_train.evaluate(net, list(seeds), fine, factor, horizons, log=None)
     r = rep["runs"][0]
-    out.update({"fine_ms": r["fine_ms"], "closure_ms": r["closure"]["wall_ms"], "plain_coarse_ms": r["plain"]["wall_ms"],
-                "closure_divb_max": r["closure"]["divb_max"], "closure_fallbacks": r["closure"]["fallbacks"],
-                "closure_steps": r["closure"]["steps"]})
+    out = {"workload": f"vortex seeds {list(seeds)}, {fine}^3 plain vs {fine // factor}^3 plain and "
+                       f"{fine // factor}^3 + closure, horizons {list(horizons)} crossing times",
+           "fine_ms": r["fine_ms"], "closure_ms": r["closure"]["wall_ms"], "plain_coarse_ms": r["plain"]["wall_ms"],
+           "speedup_vs_fine": rep["summary"]["speedup_vs_fine"], "fallback_rate": rep["summary"]["fallback_rate"],
+           "closure_divb_max": r["closure"]["per_horizon"][-1]["divb_max"]}
+    for hi, h in enumerate(rep["horizons"]):
+        p_, c_ = r["plain"]["per_horizon"][hi], r["closure"]["per_horizon"][hi]
+        out[f"t{h}"] = {k: {"plain": round(p_[k], 5), "closure": round(c_[k], 5)}
+                        for k in ("rho_rel_l2", "magnetic_spectrum_err", "kinetic_spectrum_err")}
     return out
 
 

@@ -315,16 +315,18 @@ class ClosureNet:
 
 
 class Corrector:
-    """Applies a trained net to one coarse box after each plain step."""
+    """Applies a trained net to one coarse box after each plain step; `gain`
+    scales the correction (1 = as trained)."""
 
-    def __init__(self, net: ClosureNet, n: int, ecap: float = 1e-3):
+    def __init__(self, net: ClosureNet, n: int, ecap: float = 1e-3, gain: float = 1.0):
         t = net.torch
-        self.net, self.n, self.ecap = net, n, ecap
+        self.net, self.n, self.ecap, self.gain = net, n, ecap, gain
+        self.osc = t.tensor(np.asarray(net.stats.oscale) * gain, dtype=t.float32, device=net.dev)
         nv = n ** 3
         self.x = t.empty(nv * 16, dtype=t.bfloat16, device=net.dev)
         self.ut = t.empty(nv * 5, dtype=t.float32, device=net.dev)
         self.bt = t.empty(nv * 3, dtype=t.float32, device=net.dev)
-        self.flags = t.zeros(2, dtype=t.int32, device=net.dev)
+        self.flags = t.zeros(4, dtype=t.int32, device=net.dev)
         self.esum = t.zeros(8, dtype=t.float64, device=net.dev)
         self.fallbacks = t.zeros(1, dtype=t.int64, device=net.dev)
         self.applied = 0
@@ -342,8 +344,8 @@ class Corrector:
 
     def apply(self, u_ptr: int, b_ptr: int) -> None:
         """Correct the state in place with the last prediction (or fall back)."""
-        _, _, osc = self.net._stat_tensors()
-        _check(cl().mhd_cl_apply(u_ptr, b_ptr, _p(self.net.out), self.n, _p(osc), float(self.net.stats.bscale),
+        _check(cl().mhd_cl_apply(u_ptr, b_ptr, _p(self.net.out), self.n, _p(self.osc),
+                                 float(self.net.stats.bscale * self.gain),
                                  _p(self.ut), _p(self.bt), _p(self.flags), _p(self.esum), self.ecap,
                                  _p(self.fallbacks), stream_ptr()), "mhd_cl_apply")
         self.applied += 1

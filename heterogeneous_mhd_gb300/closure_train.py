@@ -210,15 +210,15 @@ def baseline_loss(ds: Dataset, idx) -> float:
 
 def _run_to(ctx: Context, tf: float, cfl: float, chunk: int, corrector=None, stream=None,
             max_steps: int = 100000) -> int:
-    """Steps until the clock reaches tf (the last step clamped) or max_steps;
-    returns the step count (max_steps or more: tf not reached).
+    """Steps from the clock's current time until it reaches tf (the last step
+    clamped) or max_steps; returns the step count (max_steps: tf not reached).
 
     With a corrector the net runs on `stream` beside the plain step: the
     step waits only for the feature kernel (the net's one read of the
     state), the correction waits for both, the next step for the correction.
     """
     torch = _torch()
-    ctx.set_time(0.0, tf)
+    ctx.set_time(ctx.time()[0], tf)
     steps = 0
     cs = torch.cuda.ExternalStream(ctx.stream())
     while True:
@@ -244,83 +244,98 @@ def _run_to(ctx: Context, tf: float, cfl: float, chunk: int, corrector=None, str
             return steps
 
 
-def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossings: float = 2.0, cfl: float = 0.7,
-             log=_log) -> dict:
+def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossings=(0.5, 1.0, 2.0),
+             cfl: float = 0.7, log=_log, gain: float = 1.0) -> dict:
+    """Held-out seeds run to each horizon (in turbulent crossing times L / v_rms)
+    three ways; errors against the filtered fine run at every horizon, GPU
+    time to the last one."""
     torch = _torch()
+    horizons = sorted(float(c) for c in (crossings if np.iterable(crossings) else [crossings]))
     nc = fine // factor
     L = cl.cl()
     f32 = dict(dtype=torch.float32, device="cuda")
-    ucr, bcr = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
     uci, bci = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    ucr, bcr = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
     side = torch.cuda.Stream()
     res = []
     for seed in seeds:
         u, b = init_vortex(fine, fine, fine, seed=seed)
         vr = v_rms(u)
-        tf_fine = crossings * fine / vr  # crossing time L / v_rms in fine grid units
-        # fine plain run
-        with Context(fine, fine, fine) as cf:
+        t_of = [h * fine / vr for h in horizons]  # fine grid units
+        out = {"seed": seed, "v_rms": vr, "horizons": horizons}
+        refs = []
+        with Context(fine, fine, fine) as cf:  # the fine plain run, filtered at every horizon
             cf.set_state(u, b)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             st = torch.cuda.ExternalStream(cf.stream())
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             ev[0].record(st)
-            nfine = _run_to(cf, tf_fine, cfl, 4)
+            nfine = 0
+            for tf in t_of:
+                nfine += _run_to(cf, tf, cfl, 4)
+                cf.sync()
+                fu, fb = cf.state_ptrs()
+                _check(L.mhd_cl_filter(fu, fb, fine, factor, ucr.data_ptr(), bcr.data_ptr(), cl.stream_ptr()),
+                       "filter")
+                torch.cuda.synchronize()
+                ru, rb = ucr.cpu().numpy(), bcr.cpu().numpy()
+                refs.append((ru, rb, energy_spectra(ru, rb, nc)))
             ev[1].record(st)
             cf.sync()
-            ms_fine = ev[0].elapsed_time(ev[1])
-            fu, fb = cf.state_ptrs()
-            _check(L.mhd_cl_filter(fu, fb, fine, factor, ucr.data_ptr(), bcr.data_ptr(), cl.stream_ptr()), "filter")
-            torch.cuda.synchronize()
-        # coarse initial state = filtered fine initial state
+            out["fine_steps"], out["fine_ms"] = nfine, ev[0].elapsed_time(ev[1])
         du, db = torch.from_numpy(u).to("cuda"), torch.from_numpy(b).to("cuda")
         _check(L.mhd_cl_filter(du.data_ptr(), db.data_ptr(), fine, factor, uci.data_ptr(), bci.data_ptr(),
                                cl.stream_ptr()), "filter")
         torch.cuda.synchronize()
-        out = {"seed": seed, "v_rms": vr, "t_fine": tf_fine, "fine_steps": nfine, "fine_ms": ms_fine}
-        ref_u, ref_b = ucr.cpu().numpy(), bcr.cpu().numpy()
-        ref_spec = energy_spectra(ref_u, ref_b, nc)
         for label, use in (("plain", False), ("closure", True)):
+            rows = []
             with Context(nc, nc, nc) as cc:
                 _set_state_dev(cc, uci.data_ptr(), bci.data_ptr())
-                corr = cl.Corrector(net, nc) if use else None
-                st = torch.cuda.ExternalStream(cc.stream())
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                torch.cuda.synchronize()
-                ev[0].record(st)
-                t_host = time.perf_counter()
-                cap = 10000 if not use else 4 * out["plain"]["steps"] + 64
-                nst = _run_to(cc, tf_fine / factor, cfl, 8, corrector=corr, stream=side, max_steps=cap)
-                ev[1].record(st)
-                cc.sync()
-                torch.cuda.synchronize()
-                wall = (time.perf_counter() - t_host) * 1e3
-                cu_, cb_ = cc.get_state()
-                divb = cc.divb_max()
-                done = reached(cc.time()[0], tf_fine / factor)
-            spec = energy_spectra(cu_, cb_, nc)
-            errs = field_errors(cu_, cb_, ref_u, ref_b)
-            U = cu_.reshape(-1, 5)
-            out[label] = {
-                "steps": nst, "ms": ev[0].elapsed_time(ev[1]), "wall_ms": wall, "reached_t": bool(done),
-                "rho_rel_l2": errs["rho"], "field_errors": errs,
-                "kinetic_spectrum_err": spectrum_error(spec["kinetic"], ref_spec["kinetic"], nc // 2),
-                "magnetic_spectrum_err": spectrum_error(spec["magnetic"], ref_spec["magnetic"], nc // 2),
-                "divb_max": divb, "rho_min": float(U[:, 0].min()),
-                "fallbacks": corr.fallback_count() if corr else 0,
-            }
+                corr = cl.Corrector(net, nc, gain=gain) if use else None
+                nst, wall = 0, 0.0
+                for hi, tf in enumerate(t_of):
+                    cap = 100000 if not use else 4 * out["plain"]["per_horizon"][hi]["steps"] + 64
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    k = _run_to(cc, tf / factor, cfl, 8, corrector=corr, stream=side, max_steps=cap)
+                    cc.sync()
+                    torch.cuda.synchronize()
+                    wall += (time.perf_counter() - t0) * 1e3
+                    nst += k
+                    cu_, cb_ = cc.get_state()
+                    ru, rb, rspec = refs[hi]
+                    spec = energy_spectra(cu_, cb_, nc)
+                    errs = field_errors(cu_, cb_, ru, rb)
+                    rows.append({
+                        "crossings": horizons[hi], "steps": nst, "wall_ms": wall,
+                        "reached_t": bool(reached(cc.time()[0], tf / factor)),
+                        "rho_rel_l2": errs["rho"], "field_errors": errs,
+                        "kinetic_spectrum_err": spectrum_error(spec["kinetic"], rspec["kinetic"], nc // 2),
+                        "magnetic_spectrum_err": spectrum_error(spec["magnetic"], rspec["magnetic"], nc // 2),
+                        "divb_max": cc.divb_max(), "rho_min": float(cu_.reshape(-1, 5)[:, 0].min()),
+                        "fallbacks": corr.fallback_count() if corr else 0,
+                    })
+            out[label] = {"per_horizon": rows, "wall_ms": wall, "steps": nst}
         out["speedup_vs_fine"] = out["fine_ms"] / max(out["closure"]["wall_ms"], 1e-9)
         res.append(out)
         if log:
-            log(f"evaluate: seed {seed} rho L2 plain {out['plain']['rho_rel_l2']:.4f} closure "
-                f"{out['closure']['rho_rel_l2']:.4f}, Emag spec plain {out['plain']['magnetic_spectrum_err']:.4f} "
-                f"closure {out['closure']['magnetic_spectrum_err']:.4f}, fallbacks {out['closure']['fallbacks']}, "
-                f"fine {ms_fine:.0f} ms vs closure {out['closure']['wall_ms']:.0f} ms")
+            for hi, h in enumerate(horizons):
+                p_, c_ = out["plain"]["per_horizon"][hi], out["closure"]["per_horizon"][hi]
+                log(f"evaluate: seed {seed} t={h} crossings: rho L2 plain {p_['rho_rel_l2']:.4f} closure "
+                    f"{c_['rho_rel_l2']:.4f}; Emag spectrum plain {p_['magnetic_spectrum_err']:.4f} closure "
+                    f"{c_['magnetic_spectrum_err']:.4f}; Ekin spectrum plain {p_['kinetic_spectrum_err']:.4f} "
+                    f"closure {c_['kinetic_spectrum_err']:.4f}; fallbacks {c_['fallbacks']}")
+            log(f"evaluate: seed {seed} fine {out['fine_ms']:.0f} ms vs closure {out['closure']['wall_ms']:.0f} ms")
     keys = ("rho_rel_l2", "kinetic_spectrum_err", "magnetic_spectrum_err")
-    summary = {f"{lab}_{k}": float(np.mean([r[lab][k] for r in res])) for lab in ("plain", "closure") for k in keys}
-    summary["fallback_rate"] = float(np.sum([r["closure"]["fallbacks"] for r in res]) /
+    summary = {}
+    for hi, h in enumerate(horizons):
+        for lab in ("plain", "closure"):
+            for k in keys:
+                summary[f"{lab}_{k}@{h}"] = float(np.mean([r[lab]["per_horizon"][hi][k] for r in res]))
+    summary["fallback_rate"] = float(np.sum([r["closure"]["per_horizon"][-1]["fallbacks"] for r in res]) /
                                      max(1, np.sum([r["closure"]["steps"] for r in res])))
     summary["speedup_vs_fine"] = float(np.mean([r["speedup_vs_fine"] for r in res]))
-    return {"seeds": list(seeds), "fine": fine, "coarse": nc, "crossings": crossings, "summary": summary, "runs": res}
+    return {"seeds": list(seeds), "fine": fine, "coarse": nc, "horizons": horizons, "gain": gain,
+            "summary": summary, "runs": res}
 
 
 def main(argv=None):
@@ -334,7 +349,8 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-seeds", type=int, nargs="*", default=list(range(1000, 1008)))
-    ap.add_argument("--crossings", type=float, default=2.0)
+    ap.add_argument("--crossings", type=float, nargs="+", default=[0.5, 1.0, 2.0])
+    ap.add_argument("--gain", type=float, default=1.0, help="scale of the applied correction")
     ap.add_argument("--model", default="closure_model.npz")
     ap.add_argument("--load", default=None, help="skip data and training, evaluate this model")
     ap.add_argument("--report", default="closure_report.json")
@@ -357,7 +373,7 @@ def main(argv=None):
         report["stats"] = stats.to_json()
         net.save(a.model)
         del ds
-    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings)
+    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings, gain=a.gain)
     with open(a.report, "w") as f:
         json.dump(report, f, indent=1)
     print(json.dumps(report["evaluation"]["summary"]))

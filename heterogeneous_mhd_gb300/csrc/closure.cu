@@ -852,13 +852,17 @@ __global__ void k_apply0(const float* __restrict__ out, size_t nv, double* __res
     }
 }
 
-// candidate = state + correction (fluid part with its box mean removed) into (ut, bt);
-// esum[0] += sum E, esum[1] += sum E of the candidate
+// candidate = state + alpha * correction (fluid part with its box mean removed) into (ut, bt);
+// esum[0] += sum E, esum[1] += sum E of the candidate.  Nothing to do once an earlier attempt was
+// committed (flags[1]).
 __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ b, const float* __restrict__ out,
-                         int n, const float* __restrict__ oscale, float bscale, float* __restrict__ ut,
-                         float* __restrict__ bt, double* __restrict__ esum)
+                         int n, const float* __restrict__ oscale, float bscale, float alpha, float* __restrict__ ut,
+                         float* __restrict__ bt, double* __restrict__ esum, const int* __restrict__ flags)
 {
+    if (flags[1])
+        return;
     const size_t nv = (size_t)n * n * n;
+    bscale *= alpha;
     float mean[5];
 #pragma unroll
     for (int q = 0; q < 5; q++)
@@ -872,7 +876,7 @@ __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ 
         const float* ok = out + vidx(0, k + 1 == n ? 0 : k + 1, j, i, n) * 8;
 #pragma unroll
         for (int q = 0; q < 5; q++)
-            ut[v * 5 + q] = u[v * 5 + q] + oscale[q] * (o[q] - mean[q]);
+            ut[v * 5 + q] = u[v * 5 + q] + alpha * oscale[q] * (o[q] - mean[q]);
         bt[v * 3] = b[v * 3] + bscale * (-(oj[7] - o[7]) + (ok[6] - o[6]));
         bt[v * 3 + 1] = b[v * 3 + 1] + bscale * (-(ok[5] - o[5]) + (oi[7] - o[7]));
         bt[v * 3 + 2] = b[v * 3 + 2] + bscale * (-(oi[6] - o[6]) + (oj[5] - o[5]));
@@ -890,6 +894,8 @@ __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ 
 // positivity of the candidate (it needs the neighbours' candidate faces: a second pass)
 __global__ void k_apply2(const float* __restrict__ ut, const float* __restrict__ bt, int n, int* __restrict__ flags)
 {
+    if (flags[1])
+        return;
     const size_t nv = (size_t)n * n * n;
     int bad = 0;
     for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x) {
@@ -907,17 +913,22 @@ __global__ void k_apply2(const float* __restrict__ ut, const float* __restrict__
         atomicOr(flags, 1);
 }
 
-// commit the candidate unless a check failed; counts the fallbacks on the device
+// commit the candidate unless a check failed (flags[1] = 1 once committed); the last attempt
+// counts a fallback on the device when it fails too
 __global__ void k_apply3(float* __restrict__ u, float* __restrict__ b, const float* __restrict__ ut,
-                         const float* __restrict__ bt, size_t nv, const int* __restrict__ flags,
-                         const double* __restrict__ esum, float ecap, long long* __restrict__ fallbacks)
+                         const float* __restrict__ bt, size_t nv, int* __restrict__ flags,
+                         const double* __restrict__ esum, float ecap, long long* __restrict__ fallbacks, int last)
 {
+    if (flags[1])
+        return;
     const bool energy_ok = fabs(esum[1] - esum[0]) <= (double)ecap * fabs(esum[0]);
-    const bool ok = (*flags == 0) && energy_ok;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && !ok)
+    const bool ok = (flags[0] == 0) && energy_ok;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !ok && last)
         atomicAdd(reinterpret_cast<unsigned long long*>(fallbacks), 1ULL);
     if (!ok)
         return;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicExch(&flags[2], 1);  // committed: read by the next attempt's kernels as flags[1]
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nv * 5; e += (size_t)gridDim.x * blockDim.x)
         u[e] = ut[e];
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nv * 3; e += (size_t)gridDim.x * blockDim.x)
@@ -1241,22 +1252,35 @@ extern "C" MHD_API int mhd_cl_diff(const float* ua, const float* ba, const float
     return st(cudaGetLastError());
 }
 
+// between attempts: committed -> flags[1]; clear the failure bit and the energy sums
+__global__ void k_apply_next(int* flags, double* esum)
+{
+    flags[1] = flags[2];
+    flags[0] = 0;
+    esum[0] = esum[1] = 0.0;
+}
+
 extern "C" MHD_API int mhd_cl_apply(float* u, float* b, const float* out, int n, const float* oscale, float bscale,
                                     float* u_tmp, float* b_tmp, int* flags, double* esum, float ecap,
                                     long long* fallbacks, void* stream)
 {
+    const float alphas[3] = {1.0f, 0.5f, 0.25f};
     if (!u || !b || !out || !oscale || !u_tmp || !b_tmp || !flags || !esum || !fallbacks || n <= 0)
         return MHD_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t nv = (size_t)n * n * n;
-    if (cudaMemsetAsync(flags, 0, sizeof(int), s) != cudaSuccess ||
+    if (cudaMemsetAsync(flags, 0, 4 * sizeof(int), s) != cudaSuccess ||
         cudaMemsetAsync(esum, 0, 8 * sizeof(double), s) != cudaSuccess)
         return MHD_ERR_CUDA;
     const unsigned blocks = blocks_for(nv, 256);
     k_apply0<<<blocks, 256, 0, s>>>(out, nv, esum);
-    k_apply1<<<blocks, 256, 0, s>>>(u, b, out, n, oscale, bscale, u_tmp, b_tmp, esum);
-    k_apply2<<<blocks, 256, 0, s>>>(u_tmp, b_tmp, n, flags);
-    k_apply3<<<blocks, 256, 0, s>>>(u, b, u_tmp, b_tmp, nv, flags, esum, ecap, fallbacks);
+    for (int a = 0; a < 3; a++) {  // the full correction, else half, else a quarter, else none
+        if (a)
+            k_apply_next<<<1, 1, 0, s>>>(flags, esum);
+        k_apply1<<<blocks, 256, 0, s>>>(u, b, out, n, oscale, bscale, alphas[a], u_tmp, b_tmp, esum, flags);
+        k_apply2<<<blocks, 256, 0, s>>>(u_tmp, b_tmp, n, flags);
+        k_apply3<<<blocks, 256, 0, s>>>(u, b, u_tmp, b_tmp, nv, flags, esum, ecap, fallbacks, a == 2);
+    }
     return st(cudaGetLastError());
 }
 

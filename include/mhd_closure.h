@@ -67,11 +67,12 @@ MHD_API int mhd_cl_filter(const float *u_fine, const float *b_fine, int n_fine, 
 /* d[n^3][8] = (ua - ub, ba - bb) */
 MHD_API int mhd_cl_diff(const float *ua, const float *ba, const float *ub, const float *bb, int n, float *d,
                         void *stream);
-/* correction step on one box: u += oscale * (out[0..4] - its box mean), b += bscale * (-curl E),
- * E = out[5..7] (removing the means conserves mass, momentum and energy); the candidate is committed
- * only if rho > 0 and p > 0 in every cell and the total energy moves by at most ecap of itself;
- * otherwise the state is left as it is and *fallbacks is incremented.
- * u_tmp, b_tmp: candidate buffers; flags: 1 int; esum: 8 doubles. */
+/* correction step on one box: u += a oscale (out[0..4] - its box mean), b += a bscale (-curl E),
+ * E = out[5..7] (removing the means conserves mass, momentum and energy), for a = 1, else 1/2, else
+ * 1/4: the first candidate with rho > 0 and p > 0 in every cell and a total energy that moves by at
+ * most ecap of itself is committed; if none is, the state is left as it is and *fallbacks is
+ * incremented.  All on the device (no host synchronisation).
+ * u_tmp, b_tmp: candidate buffers; flags: 4 ints; esum: 8 doubles. */
 MHD_API int mhd_cl_apply(float *u, float *b, const float *out, int n, const float *oscale, float bscale,
                          float *u_tmp, float *b_tmp, int *flags, double *esum, float ecap,
                          long long *fallbacks, void *stream);

@@ -200,13 +200,13 @@ def targets(u_fine_next, b_fine_next, u_coarse, b_coarse, n, oscale, bscale):
     return t
 
 
-def apply_correction(u, b, out, n, oscale, bscale):
-    """u + oscale * (out[:5] - box mean); b + bscale * curl_faces(out[5:])."""
+def apply_correction(u, b, out, n, oscale, bscale, alpha=1.0):
+    """u + alpha oscale (out[:5] - box mean); b + alpha bscale curl_faces(out[5:])."""
     U, B = state_arrays(u, b, n)
     O = np.asarray(out, dtype=np.float64).reshape(n, n, n, 8)
     fl = O[..., :5] - O[..., :5].mean(axis=(0, 1, 2))
-    U2 = U + fl * np.asarray(oscale)
-    B2 = B + bscale * curl_faces(O[..., 5:])
+    U2 = U + alpha * fl * np.asarray(oscale)
+    B2 = B + alpha * bscale * curl_faces(O[..., 5:])
     return U2.reshape(-1), B2.reshape(-1)
 
 

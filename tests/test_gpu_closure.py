@@ -178,7 +178,7 @@ def test_correction_keeps_div_b_and_falls_back(clos, mhd, cuda):
     ud, bd, od, sd = to_f32(torch, u), to_f32(torch, b), to_f32(torch, out), to_f32(torch, osc)
     ut = torch.empty_like(ud)
     bt = torch.empty_like(bd)
-    flags = torch.zeros(2, dtype=torch.int32, device="cuda")
+    flags = torch.zeros(4, dtype=torch.int32, device="cuda")
     esum = torch.zeros(8, dtype=torch.float64, device="cuda")
     fb = torch.zeros(1, dtype=torch.int64, device="cuda")
     args = (ut.data_ptr(), bt.data_ptr(), flags.data_ptr(), esum.data_ptr(), 1e-2, fb.data_ptr(), s)
@@ -188,7 +188,23 @@ def test_correction_keeps_div_b_and_falls_back(clos, mhd, cuda):
     assert rel(ud.cpu().numpy(), ur) < 1e-6 and rel(bd.cpu().numpy(), br) < 1e-6
     assert int(fb.item()) == 0
     assert mhd.host_divb_max(bd.cpu().numpy(), n, n, n) < 1e-5  # CT update: div B at FP32 round-off
-    # a correction that makes rho negative somewhere is refused
+    # a correction whose full size breaks positivity is applied at the first of 1/2, 1/4 that keeps it
+    part = out.copy()
+    part[2, 2, 2, 0] = -1.2 / osc[0]  # rho ~ 1 - 1.2 < 0 at full size
+    u_h, b_h = ud.cpu().numpy().copy(), bd.cpu().numpy().copy()
+    expect = None
+    for alpha in (1.0, 0.5, 0.25):
+        uc, bc = co.apply_correction(u_h, b_h, part, n, osc, bscale, alpha=alpha)
+        if uc.reshape(-1, 5)[:, 0].min() > 0 and co.pressure(uc, bc, n).min() > 0:
+            expect = (alpha, uc, bc)
+            break
+    assert expect is not None and expect[0] < 1.0
+    od_h = to_f32(torch, part)
+    assert L.mhd_cl_apply(ud.data_ptr(), bd.data_ptr(), od_h.data_ptr(), n, sd.data_ptr(), bscale, *args) == 0
+    torch.cuda.synchronize()
+    assert rel(ud.cpu().numpy(), expect[1]) < 1e-6 and rel(bd.cpu().numpy(), expect[2]) < 1e-6
+    assert int(fb.item()) == 0
+    # a correction that makes rho negative even at a quarter of its size is refused
     bad = out.copy()
     bad[3, 4, 5, 0] = -10.0
     u1, b1 = ud.cpu().numpy().copy(), bd.cpu().numpy().copy()
