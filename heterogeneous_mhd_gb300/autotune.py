@@ -21,7 +21,7 @@ from pathlib import Path
 from . import Context, init_turbulence, lib
 
 CACHE = Path(os.environ.get("MHD_GB300_TUNE_CACHE", Path(__file__).resolve().parent / "lib" / "tuning.json"))
-KNOBS = ("fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K")
+KNOBS = ("fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K", "fluidx.cells")
 
 
 def set_knob(key: str, value: int) -> None:
@@ -63,7 +63,9 @@ def _time_kernel(ctx: Context, kernel: str, steps: int) -> float:
 
 def candidates(n: int):
     """(knob settings) to try for fluidx and for advectbyzx on an n^3 grid."""
-    fx = [{"fluidx.threads": t} for t in (64, 128, 256)]
+    fx = [{"fluidx.threads": t, "fluidx.cells": 4} for t in (64, 128, 256)]
+    if n % 8 == 0 and 8 <= n // 8 <= 64 and (n // 8) & (n // 8 - 1) == 0:
+        fx += [{"fluidx.threads": t, "fluidx.cells": 8} for t in (32, 64, 128, 256) if t >= n // 8]
     adv = []
     for cells in (4, 8):
         t = n // cells

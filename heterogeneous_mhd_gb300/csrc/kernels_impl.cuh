@@ -56,13 +56,15 @@ static FxPlan plan_fluidx(int nx, int ny, bool aligned)
 {
     FxPlan p{0, 0, 0};
     if (kV2 && aligned) {
-        if (nx % 4 == 0 && pow2_in(nx / 4, 8, 128))
+        if (tune_value(TUNE_FLUIDX_C) == 8 && nx % 8 == 0 && pow2_in(nx / 8, 8, 64))
+            p.C = 8, p.T = nx / 8;
+        else if (nx % 4 == 0 && pow2_in(nx / 4, 8, 128))
             p.C = 4, p.T = nx / 4;
         else if (nx % 3 == 0 && nx % 4 == 0 && pow2_in(nx / 3, 16, 128))
             p.C = 3, p.T = nx / 3;
         if (p.C) {
             int target = tune_value(TUNE_FLUIDX_THREADS);
-            if (target != 64 && target != 128 && target != 256)
+            if (target != 32 && target != 64 && target != 128 && target != 256)
                 target = 64;  // measured best on GB300 at 256^3 (autotune.py)
             p.P = 0;
             for (int P = 1; P <= ny; P++)
@@ -147,7 +149,14 @@ static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
     const FxPlan p = plan_fluidx(a.nx, a.ny, a.use_tma != 0);
     a.P = p.P;
     if constexpr (kV2) {
-        if (p.C == 4) {
+        if (p.C == 8) {
+            switch (p.T) {
+            case 8: return launch_fx2<8, 8>(a, s);
+            case 16: return launch_fx2<8, 16>(a, s);
+            case 32: return launch_fx2<8, 32>(a, s);
+            case 64: return launch_fx2<8, 64>(a, s);
+            }
+        } else if (p.C == 4) {
             switch (p.T) {
             case 8: return launch_fx2<4, 8>(a, s);
             case 16: return launch_fx2<4, 16>(a, s);

@@ -180,13 +180,8 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         tvdb_row<R, EX, C, T>(g, vr, bv, dt, seam, F, bn);
         if (brow) {
             const int pb = k0 & 1;
-            float* fbw = FB + ((size_t)pb * J + bp) * n + g.t * C;
-            float* b3w = B3 + ((size_t)pb * J + bp) * n + g.t * C;
-#pragma unroll
-            for (int m = 0; m < C; m++) {
-                fbw[m] = F[m];
-                b3w[m] = bn[m];
-            }
+            sts_chunk<float, C>(FB + ((size_t)pb * J + bp) * n + g.t * C, F);  // one 16-byte store per row
+            sts_chunk<float, C>(B3 + ((size_t)pb * J + bp) * n + g.t * C, bn);
         }
     }
     __syncthreads();
@@ -228,9 +223,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         const int pk = k & 1, pk1 = (k + 1) & 1;
         if (live) {
             float* w = (r <= J) ? FA + (size_t)r * n + g.t * C : FB + ((size_t)pk1 * J + bp) * n + g.t * C;
-#pragma unroll
-            for (int m = 0; m < C; m++)
-                w[m] = F[m];
+            sts_chunk<float, C>(w, F);
         }
         __syncthreads();
         if (NS == 2 && k + 2 <= k0 + K) {  // plane k has been read: refill its slot
@@ -247,10 +240,11 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
                 for (int m = 0; m < C; m++)
                     b1own[m] = b1c[3 * m];
             }
-            const float* fa1 = FA + (size_t)(r + 1) * n + g.t * C;
-            const float* fb = FB + ((size_t)pk * J + r) * n + g.t * C;
-            const float* fbp = FB + ((size_t)pk1 * J + r) * n + g.t * C;
-            const float* b3 = B3 + ((size_t)pk * J + r) * n + g.t * C;
+            float fa1[C], fb[C], fbp[C], b3[C];  // 16-byte loads: no bank conflicts for C = 4
+            lds_chunk<float, C>(FA + (size_t)(r + 1) * n + g.t * C, fa1);
+            lds_chunk<float, C>(FB + ((size_t)pk * J + r) * n + g.t * C, fb);
+            lds_chunk<float, C>(FB + ((size_t)pk1 * J + r) * n + g.t * C, fbp);
+            lds_chunk<float, C>(B3 + ((size_t)pk * J + r) * n + g.t * C, b3);
             float out[C * 3];
 #pragma unroll
             for (int m = 0; m < C; m++) {
@@ -275,12 +269,8 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
                             blockDim.x);
         }
         // the B rows' advected b(3) of plane k+1, for the next step
-        if (brow) {
-            float* b3w = B3 + ((size_t)pk1 * J + bp) * n + g.t * C;
-#pragma unroll
-            for (int m = 0; m < C; m++)
-                b3w[m] = bn[m];
-        }
+        if (brow)
+            sts_chunk<float, C>(B3 + ((size_t)pk1 * J + bp) * n + g.t * C, bn);
         __syncthreads();
     }
 }

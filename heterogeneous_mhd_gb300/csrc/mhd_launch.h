@@ -44,6 +44,7 @@ enum TuneKey : int {
     TUNE_ADVECT_SLOTS,        // plane-slab ring depth (2 or 3)
     TUNE_ADVECT_J,            // pencils per CTA along j
     TUNE_ADVECT_K,            // planes per CTA along k
+    TUNE_FLUIDX_C,            // cells per thread of the register-resident fluidx (4, or 8: one warp per pencil)
     TUNE_COUNT
 };
 int tune_value(int key);

@@ -183,3 +183,24 @@ def test_full_size_512_properties(mhd, cuda):
     m0 = u0.reshape(-1, 5)[:, 0].astype(np.float64).sum()
     m1 = uf.reshape(-1, 5)[:, 0].astype(np.float64).sum()
     assert abs(m1 - m0) <= 1e-5 * m0
+
+
+@pytest.mark.parametrize("knobs", [{"fluidx.cells": 8, "fluidx.threads": 32}, {"fluidx.cells": 8, "fluidx.threads": 64},
+                                   {"advect.cells": 8}])
+def test_launch_shapes_do_not_change_results(knobs, mhd, cuda):
+    """Every launch shape the tuner may pick computes the same numbers: the
+    EXACT kernels reproduce the reference checksums of the 64^3 vortex and the
+    FAST kernels match the default shapes bit for bit at 128^3."""
+    from heterogeneous_mhd_gb300 import autotune
+    ck = checksums()["f32"]
+    u0, b0 = mhd.init_vortex(64, 64, 64, seed=0)
+    ut, bt = mhd.init_turbulence(128, seed=2)
+    ref_fast = run(mhd, ut, bt, (128, 128, 128), 3)
+    try:
+        autotune.apply(knobs)
+        u, b, _ = run(mhd, u0, b0, (64, 64, 64), 10, exact=True)
+        assert sha(u, b) == ck["10"]["sha256"]
+        uf, bf, _ = run(mhd, ut, bt, (128, 128, 128), 3)
+        assert bitwise_equal(uf, ref_fast[0]) and bitwise_equal(bf, ref_fast[1])
+    finally:
+        autotune.apply({k: 0 for k in knobs})
