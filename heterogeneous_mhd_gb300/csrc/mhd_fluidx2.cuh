@@ -34,7 +34,7 @@ __host__ __device__ inline size_t fluidx2_smem_elems(int n, int P, int ax = 0)
 }
 
 template <typename R, bool EX, int C, int T, int AX = 0>
-__global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
+__global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
 {
     select_box(a, blockIdx.z, sizeof(CflPart<R>));
     constexpr int n = C * T;
@@ -161,12 +161,12 @@ __global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
                     gl[m][s] = scale0<R, EX>(c, lin<R, EX>(R(1), q[m][s], R(-1), v[m][s]));
                 }
             } else {
-                // c*(u +- v/c) = c*u +- v when c > 0; both vanish when c == 0
-                const bool pos = c > R(0);
+                // c*(u +- v/c) = c*u +- v.  c == 0 only when every cell of the pencil has zero
+                // velocity and zero magnetosonic speed, where the fluxes v vanish too.
 #pragma unroll
                 for (int s = 0; s < 5; s++) {
-                    fr[m][s] = pos ? fma(c, q[m][s], v[m][s]) : R(0);
-                    gl[m][s] = pos ? fma(c, q[m][s], -v[m][s]) : R(0);
+                    fr[m][s] = fma(c, q[m][s], v[m][s]);
+                    gl[m][s] = fma(c, q[m][s], -v[m][s]);
                 }
             }
         }
@@ -212,11 +212,10 @@ __global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
                     gl[m][s] = scale0<R, EX>(c, lin<R, EX>(R(1), u1[m][s], R(-1), v[m][s]));
                 }
             } else {
-                const bool pos = c > R(0);
 #pragma unroll
                 for (int s = 0; s < 5; s++) {
-                    fr[m][s] = pos ? fma(c, u1[m][s], v[m][s]) : R(0);
-                    gl[m][s] = pos ? fma(c, u1[m][s], -v[m][s]) : R(0);
+                    fr[m][s] = fma(c, u1[m][s], v[m][s]);
+                    gl[m][s] = fma(c, u1[m][s], -v[m][s]);
                 }
             }
         }
@@ -253,9 +252,11 @@ __global__ void __launch_bounds__(256, AX ? 3 : 1) k_fluidx2(FluidxArgs a)
                     dfr = vanleer<R, EX>(dmn, dm[m][s]);
                     dfl = vanleer<R, EX>(dln, dl[m][s]);
                 } else {
+                    // branch-free: the quotient is computed for every cell and selected
                     const R pr = dmn * dm[m][s], pl = dln * dl[m][s];
-                    dfr = (pr > R(0)) ? fast_div(R(2) * pr, dmn + dm[m][s]) : R(0);
-                    dfl = (pl > R(0)) ? fast_div(R(2) * pl, dln + dl[m][s]) : R(0);
+                    const R qr = fast_div(R(2) * pr, dmn + dm[m][s]), ql = fast_div(R(2) * pl, dln + dl[m][s]);
+                    dfr = (pr > R(0)) ? qr : R(0);
+                    dfl = (pl > R(0)) ? ql : R(0);
                 }
                 const R gn = (m + 1 < C) ? gl[m + 1][s] : gln[s];
                 flux[m][s] = lin<R, EX>(R(0.5), lin<R, EX>(R(1), fr[m][s], R(-1), gn), R(0.5),

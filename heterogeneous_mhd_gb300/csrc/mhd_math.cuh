@@ -92,14 +92,16 @@ template <typename R, bool EX>
 __device__ __forceinline__ R vanleer(R a, R b)
 {
     using W = wide_t<R, EX>;
-    R r = R(0);
-    if (a * b > R(0)) {
-        if constexpr (EX)
+    if constexpr (EX) {
+        R r = R(0);
+        if (a * b > R(0))
             r = R(W(2.0) * W(a) * W(b) / W(a + b));
-        else
-            r = fast_div(R(2) * a * b, a + b);
+        return r;
+    } else {  // branch-free: quotient for every cell, then the select
+        const R ab = a * b;
+        const R q = fast_div(R(2) * ab, a + b);
+        return (ab > R(0)) ? q : R(0);
     }
-    return r;
 }
 
 // mhdflux for one cell (C/mhdflux.c:21-46): flux v (before division by the
