@@ -140,14 +140,21 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T>& g, const R (&vr)[C],
             const R vbp = (m + 1 < C) ? vb[m + 1] : xr[0];
             const R vbpp = (m + 2 < C) ? vb[m + 2] : ((m + 2 == C) ? xr[0] : xr[1]);
             R w, wp, wm;
-            if (vh[m] > R(0)) {
-                w = vb[m];
-                wp = R(W(vbp - w) / W(2.0));
-                wm = R(W(w - vbm) / W(2.0));
-            } else {
-                w = vbp;
-                wp = R(W(w - vbpp) / W(2.0));
-                wm = R(W(vb[m] - w) / W(2.0));
+            if constexpr (EX) {
+                if (vh[m] > R(0)) {
+                    w = vb[m];
+                    wp = R(W(vbp - w) / W(2.0));
+                    wm = R(W(w - vbm) / W(2.0));
+                } else {
+                    w = vbp;
+                    wp = R(W(w - vbpp) / W(2.0));
+                    wm = R(W(vb[m] - w) / W(2.0));
+                }
+            } else {  // the same differences with the operands selected: no branch
+                const bool up = vh[m] > R(0);
+                w = up ? vb[m] : vbp;
+                wp = (vbp - (up ? vb[m] : vbpp)) * R(0.5);
+                wm = (vb[m] - (up ? vbm : vbp)) * R(0.5);
             }
             const R dw = vanleer<R, EX>(wm, wp);
             flux[m] = (w + dw) * dt;
