@@ -73,8 +73,8 @@ __device__ __forceinline__ void stg_chunk(R* dst, const R (&src)[NF])
 // smoothing (C/advectbyzxA1.c:36-41) and tvdb (C/tvdb.c:10-91).  Returns
 // F(i) = flux(i-1) (the EMF times dt used by the CT update) and the advected
 // field.  Seven neighbour exchanges; for T > 32 each is one block barrier.
-template <typename R, bool EX, int C, int T>
-__device__ __forceinline__ void tvdb_row(const Group<R, T>& g, const R (&vr)[C], const R (&bv)[C], R dt, R* seam,
+template <typename R, bool EX, int C, int T, bool NM>
+__device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)[C], const R (&bv)[C], R dt, R* seam,
                                          R (&F)[C], R (&bnew)[C])
 {
     using W = wide_t<R, EX>;

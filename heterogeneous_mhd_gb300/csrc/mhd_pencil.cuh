@@ -154,7 +154,7 @@ __device__ __forceinline__ void sts_chunk(R* dst, const R (&src)[NF])
 // Exchange helper for one group of T threads (T a power of two <= 32, or a
 // multiple of 32).  `seam` is this CTA's scratch for warp-seam values: two
 // alternating banks of [warps][kSeamVals] elements.
-template <typename R, int T>
+template <typename R, int T, bool kNamed = false>
 struct Group {
     static constexpr bool kMulti = (T > 32);
     static constexpr int kWarps = kMulti ? T / 32 : 1;
@@ -173,6 +173,19 @@ struct Group {
         gwarp0 = warp - (t >> 5);
     }
 
+    // kNamed: the barrier of this group's T threads only (named barrier 1 + group
+    // index; 0 is __syncthreads'), so that the row groups of a CTA do not wait for
+    // one another; otherwise the CTA barrier (a CTA that is one group).
+    __device__ __forceinline__ void sync() const
+    {
+        if constexpr (kNamed) {
+            __syncwarp();
+            asm volatile("barrier.sync %0, %1;" ::"r"(1 + gwarp0 / kWarps), "r"(T) : "memory");
+        } else {
+            __syncthreads();
+        }
+    }
+
     // Max over the group's values (starting from 0, NaN skipped as by fmax).
     __device__ __forceinline__ R max(R x, R* red) const
     {
@@ -183,7 +196,7 @@ struct Group {
         if constexpr (kMulti) {
             if (lane == 0)
                 red[warp] = x;
-            __syncthreads();
+            sync();
             R m = R(0);
 #pragma unroll
             for (int s = 0; s < kWarps; s++)
@@ -206,24 +219,24 @@ struct Group {
                 out[k] = __shfl_sync(kFull, x[k], src, T);
         } else {
             static_assert(K <= kSeamVals, "too many values per exchange");
-            R* s = seam + bank * (32 * kSeamVals);  // [warp][K], fixed bank stride
+            R* s = seam + bank * (32 * kSeamVals);  // [warp][kSeamVals]: slots independent of K
             const int edge = (dir > 0) ? 0 : 31;     // the lane whose value crosses the seam
             if (lane == edge) {
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                    s[warp * K + k] = x[k];
+                    s[warp * kSeamVals + k] = x[k];
             }
 #pragma unroll
             for (int k = 0; k < K; k++)
                 out[k] = (dir > 0) ? __shfl_down_sync(kFull, x[k], 1) : __shfl_up_sync(kFull, x[k], 1);
-            __syncthreads();
+            sync();
             const int need = (dir > 0) ? 31 : 0;
             if (lane == need) {
                 const int gw = warp - gwarp0;
                 const int nb = (dir > 0) ? ((gw + 1) % kWarps) : ((gw + kWarps - 1) % kWarps);
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                    out[k] = s[(gwarp0 + nb) * K + k];
+                    out[k] = s[(gwarp0 + nb) * kSeamVals + k];
             }
         }
     }
