@@ -275,15 +275,14 @@ def our_arm(args):
 
     import heterogeneous_mhd_gb300 as mhd
 
+    from heterogeneous_mhd_gb300.replicas import Replicas
+
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    rep = Replicas("nccl")
     n = args.size
     cells = n ** 3
-    u0, b0 = mhd.init_turbulence(n, seed=rank)
+    u0, b0 = mhd.init_turbulence(n, seed=rep.seed())
     tuned = {}
     if not args.no_tune:  # time the launch-shape candidates on this device first
         from heterogeneous_mhd_gb300 import autotune
@@ -296,8 +295,7 @@ def our_arm(args):
     def barrier():
         ctx.sync()
         torch.cuda.synchronize()
-        if dist is not None:
-            dist.barrier()
+        rep.barrier()
 
     # warm-up (also captures the step graph), then one step through the
     # profiled direct-launch path so the timed region starts warm on it too
@@ -334,12 +332,7 @@ def our_arm(args):
         ctx.profile(False)
         status = ctx.check()
 
-    t_max = ms
-    if dist is not None:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt[0])
-    value = world * cells * args.steps / (t_max * 1e-3)
+    value, t_max = rep.throughput(cells, args.steps, ms)
 
     # e2e: host state in and out of the C ABI every step
     hu = torch.empty(5 * cells, dtype=torch.float32, pin_memory=True)
@@ -354,10 +347,7 @@ def our_arm(args):
         ctx.step(1, cfl=0.7, fused=fused)
         ctx.get_state_into(hu, hb)  # D2H, synchronises
     e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt[0])
+    (e2e_s,) = rep.max([e2e_s])
     e2e = world * cells * e2e_steps / e2e_s
 
     # roofline of the dominant kernel
@@ -370,8 +360,7 @@ def our_arm(args):
     step_bw = STEP_BYTES[args.variant] * cells / (ms / args.steps * 1e-3) / 1e9
     if rank != 0:
         ctx.close()
-        if dist is not None:
-            dist.destroy_process_group()
+        rep.close()
         return
     share = {k: round(v[0] / sum(x[0] for x in kern.values()), 4) for k, v in kern.items() if v[1] > 0}
     line = {
@@ -404,8 +393,7 @@ def our_arm(args):
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n)
     print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    rep.close()
 
 
 def ncu_case(args):
