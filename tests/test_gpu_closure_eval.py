@@ -20,8 +20,8 @@ def test_trained_closure_beats_plain_coarse(mhd, cuda):
     net = closure.ClosureNet.load(WEIGHTS)
     rep = closure_train.evaluate(net, [1000], fine=256, factor=4, crossings=[0.5], log=None)
     s = rep["summary"]
-    out = Path(os.environ.get("GRAFT_REPO_ROOT", ".")) / "gpurun_out"
-    if out.is_dir():
+    out = Path(os.environ.get("MHD_METRICS_DIR", "")) if os.environ.get("MHD_METRICS_DIR") else None
+    if out is not None and out.is_dir():
         (out / "closure_eval_test.json").write_text(json.dumps(s, indent=1))
     assert s["closure_rho_rel_l2@0.5"] < s["plain_rho_rel_l2@0.5"]
     assert s["closure_magnetic_spectrum_err@0.5"] < s["plain_magnetic_spectrum_err@0.5"]

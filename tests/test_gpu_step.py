@@ -37,8 +37,8 @@ def run(mhd, u0, b0, shape, nsteps, exact=False, fp64=False, cfl=0.7, graphs=Tru
 
 
 def record(name, value):
-    out = Path(os.environ.get("GRAFT_REPO_ROOT", ".")) / "gpurun_out"
-    if out.is_dir():
+    out = Path(os.environ.get("MHD_METRICS_DIR", "")) if os.environ.get("MHD_METRICS_DIR") else None
+    if out is not None and out.is_dir():
         p = out / "parity_metrics.json"
         d = json.loads(p.read_text()) if p.exists() else {}
         d[name] = value
