@@ -86,6 +86,7 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
         "mhd_set_state": (C.c_int, [_vp, _vp, _vp, C.c_int]),
         "mhd_get_state": (C.c_int, [_vp, _vp, _vp, C.c_int]),
         "mhd_state_ptrs": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+        "mhd_clock_ptr": (C.c_int, [_vp, C.POINTER(_vp)]),
         "mhd_step": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
         "mhd_set_time": (C.c_int, [_vp, C.c_double, C.c_double]),
         "mhd_get_time": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -272,6 +273,12 @@ class Context:
     def get_state_into(self, u, b) -> None:
         where = self._where(u)
         _check(lib().mhd_get_state(self._h, _ptr(u), _ptr(b), where), "mhd_get_state")
+
+    def clock_ptr(self) -> int:
+        """Device address of the step clock (t, tf, dt, 1/c)."""
+        p = C.c_void_p()
+        _check(lib().mhd_clock_ptr(self._h, C.byref(p)), "mhd_clock_ptr")
+        return p.value
 
     def state_ptrs(self):
         pu, pb = C.c_void_p(), C.c_void_p()

@@ -63,7 +63,7 @@ def _sig():
         "mhd_cl_moments": (i, [vp, i, ll, vp, vp]),
         "mhd_cl_filter": (i, [vp, vp, i, i, vp, vp, vp]),
         "mhd_cl_diff": (i, [vp, vp, vp, vp, i, vp, vp]),
-        "mhd_cl_apply": (i, [vp, vp, vp, i, vp, f, vp, vp, vp, vp, f, vp, vp]),
+        "mhd_cl_apply": (i, [vp, vp, vp, i, vp, f, vp, vp, vp, vp, f, vp, vp, f, vp]),
         "mhd_cl_adamw": (i, [vp, vp, vp, vp, ll, i, f, f, f, f, f, vp]),
         "mhd_cl_pack": (i, [vp, i, i, i, i, i, vp, vp, vp]),
         "mhd_cl_use_tcgen05": (i, [i]),
@@ -342,12 +342,13 @@ class Corrector:
         self.features(u_ptr, b_ptr)
         self.forward()
 
-    def apply(self, u_ptr: int, b_ptr: int) -> None:
-        """Correct the state in place with the last prediction (or fall back)."""
+    def apply(self, u_ptr: int, b_ptr: int, dt_ptr: int | None = None, dt_min: float = 0.0) -> None:
+        """Correct the state in place with the last prediction (or fall back); with dt_ptr
+        (the device dt of the step just taken) nothing happens when that step was empty."""
         _check(cl().mhd_cl_apply(u_ptr, b_ptr, _p(self.net.out), self.n, _p(self.osc),
                                  float(self.net.stats.bscale * self.gain),
                                  _p(self.ut), _p(self.bt), _p(self.flags), _p(self.esum), self.ecap,
-                                 _p(self.fallbacks), stream_ptr()), "mhd_cl_apply")
+                                 _p(self.fallbacks), dt_ptr, float(dt_min), stream_ptr()), "mhd_cl_apply")
         self.applied += 1
 
     def fallback_count(self) -> int:

@@ -221,27 +221,48 @@ def _run_to(ctx: Context, tf: float, cfl: float, chunk: int, corrector=None, str
     ctx.set_time(ctx.time()[0], tf)
     steps = 0
     cs = torch.cuda.ExternalStream(ctx.stream())
-    while True:
+    dt_ptr = ctx.clock_ptr() + 2 * 4  # the clock's dt (FP32 state)
+    dt_min = 1e-6 * tf
+
+    def corrected_step():
+        up, bp = ctx.state_ptrs()
+        with torch.cuda.stream(stream):
+            stream.wait_stream(cs)
+            corrector.features(up, bp)
+            read = torch.cuda.Event()
+            read.record(stream)
+            corrector.forward()
+        cs.wait_event(read)
+        ctx.step(1, cfl=cfl)
+        with torch.cuda.stream(stream):
+            stream.wait_stream(cs)
+            corrector.apply(up, bp, dt_ptr, dt_min)
+        cs.wait_stream(stream)
+
+    graph = None
+    if corrector is not None:
+        corrected_step()  # uncaptured: the step's CFL state becomes steady, buffers exist
+        steps = 1
+        if not reached(ctx.time()[0], tf):
+            # one corrected step as one CUDA graph: the plain step as direct launches inside it
+            ctx.use_graphs(False)
+            graph = torch.cuda.CUDAGraph()
+            try:
+                with torch.cuda.graph(graph, stream=cs):
+                    corrected_step()
+            finally:
+                ctx.use_graphs(True)
+    while not (reached(ctx.time()[0], tf) or steps >= max_steps):
         if corrector is None:
             ctx.step(chunk, cfl=cfl)
-            steps += chunk
         else:
-            up, bp = ctx.state_ptrs()
-            with torch.cuda.stream(stream):
-                stream.wait_stream(cs)
-                corrector.features(up, bp)
-                read = torch.cuda.Event()
-                read.record(stream)
-                corrector.forward()
-            cs.wait_event(read)
-            ctx.step(1, cfl=cfl)
-            with torch.cuda.stream(stream):
-                stream.wait_stream(cs)
-                corrector.apply(up, bp)
-            cs.wait_stream(stream)
-            steps += 1
-        if reached(ctx.time()[0], tf) or steps >= max_steps:
-            return steps
+            # `chunk` replays per check of the clock: steps past tf have dt at round-off
+            # and the correction skips them on the device
+            with torch.cuda.stream(cs):
+                for _ in range(chunk):
+                    graph.replay()
+        steps += chunk
+    return steps
 
 
 def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossings=(0.5, 1.0, 2.0),

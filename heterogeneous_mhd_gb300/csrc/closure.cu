@@ -835,10 +835,17 @@ __global__ void k_diff(const float* __restrict__ ua, const float* __restrict__ b
 
 // ------------------------------------------------------------ correction step
 
+// The correction follows a step of length 2 dt; none when that step was empty (dt at
+// round-off: a run already at its final time).  dt may be absent (always correct).
+__device__ __forceinline__ bool skip_step(const float* dt, float dt_min) { return dt && !(*dt > dt_min); }
+
 // esum[2 + c] += sum over the box of out[.][c], c < 5 (the fluid corrections' means are removed,
 // so the correction conserves mass, momentum and energy as the filtered fine step does)
-__global__ void k_apply0(const float* __restrict__ out, size_t nv, double* __restrict__ esum)
+__global__ void k_apply0(const float* __restrict__ out, size_t nv, double* __restrict__ esum,
+                         const float* __restrict__ dt, float dt_min)
 {
+    if (skip_step(dt, dt_min))
+        return;
     double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x)
 #pragma unroll
@@ -857,9 +864,10 @@ __global__ void k_apply0(const float* __restrict__ out, size_t nv, double* __res
 // committed (flags[1]).
 __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ b, const float* __restrict__ out,
                          int n, const float* __restrict__ oscale, float bscale, float alpha, float* __restrict__ ut,
-                         float* __restrict__ bt, double* __restrict__ esum, const int* __restrict__ flags)
+                         float* __restrict__ bt, double* __restrict__ esum, const int* __restrict__ flags,
+                         const float* __restrict__ dt, float dt_min)
 {
-    if (flags[1])
+    if (flags[1] || skip_step(dt, dt_min))
         return;
     const size_t nv = (size_t)n * n * n;
     bscale *= alpha;
@@ -892,9 +900,10 @@ __global__ void k_apply1(const float* __restrict__ u, const float* __restrict__ 
 }
 
 // positivity of the candidate (it needs the neighbours' candidate faces: a second pass)
-__global__ void k_apply2(const float* __restrict__ ut, const float* __restrict__ bt, int n, int* __restrict__ flags)
+__global__ void k_apply2(const float* __restrict__ ut, const float* __restrict__ bt, int n, int* __restrict__ flags,
+                         const float* __restrict__ dt, float dt_min)
 {
-    if (flags[1])
+    if (flags[1] || skip_step(dt, dt_min))
         return;
     const size_t nv = (size_t)n * n * n;
     int bad = 0;
@@ -917,9 +926,10 @@ __global__ void k_apply2(const float* __restrict__ ut, const float* __restrict__
 // counts a fallback on the device when it fails too
 __global__ void k_apply3(float* __restrict__ u, float* __restrict__ b, const float* __restrict__ ut,
                          const float* __restrict__ bt, size_t nv, int* __restrict__ flags,
-                         const double* __restrict__ esum, float ecap, long long* __restrict__ fallbacks, int last)
+                         const double* __restrict__ esum, float ecap, long long* __restrict__ fallbacks, int last,
+                         const float* __restrict__ dt, float dt_min)
 {
-    if (flags[1])
+    if (flags[1] || skip_step(dt, dt_min))
         return;
     const bool energy_ok = fabs(esum[1] - esum[0]) <= (double)ecap * fabs(esum[0]);
     const bool ok = (flags[0] == 0) && energy_ok;
@@ -1262,7 +1272,7 @@ __global__ void k_apply_next(int* flags, double* esum)
 
 extern "C" MHD_API int mhd_cl_apply(float* u, float* b, const float* out, int n, const float* oscale, float bscale,
                                     float* u_tmp, float* b_tmp, int* flags, double* esum, float ecap,
-                                    long long* fallbacks, void* stream)
+                                    long long* fallbacks, const float* dt, float dt_min, void* stream)
 {
     const float alphas[3] = {1.0f, 0.5f, 0.25f};
     if (!u || !b || !out || !oscale || !u_tmp || !b_tmp || !flags || !esum || !fallbacks || n <= 0)
@@ -1273,13 +1283,14 @@ extern "C" MHD_API int mhd_cl_apply(float* u, float* b, const float* out, int n,
         cudaMemsetAsync(esum, 0, 8 * sizeof(double), s) != cudaSuccess)
         return MHD_ERR_CUDA;
     const unsigned blocks = blocks_for(nv, 256);
-    k_apply0<<<blocks, 256, 0, s>>>(out, nv, esum);
+    k_apply0<<<blocks, 256, 0, s>>>(out, nv, esum, dt, dt_min);
     for (int a = 0; a < 3; a++) {  // the full correction, else half, else a quarter, else none
         if (a)
             k_apply_next<<<1, 1, 0, s>>>(flags, esum);
-        k_apply1<<<blocks, 256, 0, s>>>(u, b, out, n, oscale, bscale, alphas[a], u_tmp, b_tmp, esum, flags);
-        k_apply2<<<blocks, 256, 0, s>>>(u_tmp, b_tmp, n, flags);
-        k_apply3<<<blocks, 256, 0, s>>>(u, b, u_tmp, b_tmp, nv, flags, esum, ecap, fallbacks, a == 2);
+        k_apply1<<<blocks, 256, 0, s>>>(u, b, out, n, oscale, bscale, alphas[a], u_tmp, b_tmp, esum, flags, dt,
+                                        dt_min);
+        k_apply2<<<blocks, 256, 0, s>>>(u_tmp, b_tmp, n, flags, dt, dt_min);
+        k_apply3<<<blocks, 256, 0, s>>>(u, b, u_tmp, b_tmp, nv, flags, esum, ecap, fallbacks, a == 2, dt, dt_min);
     }
     return st(cudaGetLastError());
 }

@@ -571,6 +571,14 @@ extern "C" MHD_API int mhd_state_ptrs(mhd_ctx* c, void** u, void** b)
     return set_err(MHD_OK);
 }
 
+extern "C" MHD_API int mhd_clock_ptr(mhd_ctx* c, void** clock)
+{
+    if (!c || !clock || !c->clock.p)
+        return set_err(MHD_ERR_ARG);
+    *clock = c->clock.p;
+    return set_err(MHD_OK);
+}
+
 extern "C" MHD_API int mhd_set_time(mhd_ctx* c, double t, double tf)
 {
     if (!c)

@@ -71,11 +71,13 @@ MHD_API int mhd_cl_diff(const float *ua, const float *ba, const float *ub, const
  * E = out[5..7] (removing the means conserves mass, momentum and energy), for a = 1, else 1/2, else
  * 1/4: the first candidate with rho > 0 and p > 0 in every cell and a total energy that moves by at
  * most ecap of itself is committed; if none is, the state is left as it is and *fallbacks is
- * incremented.  All on the device (no host synchronisation).
+ * incremented.  All on the device (no host synchronisation).  dt (device, may be NULL): the
+ * half step of the step just taken (the clock's dt, mhd_clock_ptr); nothing is done when it is not
+ * above dt_min (an empty step of a run already at its final time).
  * u_tmp, b_tmp: candidate buffers; flags: 4 ints; esum: 8 doubles. */
 MHD_API int mhd_cl_apply(float *u, float *b, const float *out, int n, const float *oscale, float bscale,
                          float *u_tmp, float *b_tmp, int *flags, double *esum, float ecap,
-                         long long *fallbacks, void *stream);
+                         long long *fallbacks, const float *dt, float dt_min, void *stream);
 /* AdamW with decoupled weight decay, bias-corrected moments (step >= 1) */
 MHD_API int mhd_cl_adamw(float *p, const float *g, float *m, float *v, long long count, int step, float lr,
                          float beta1, float beta2, float eps, float wd, void *stream);

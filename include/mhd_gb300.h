@@ -126,6 +126,9 @@ MHD_API int mhd_set_state(mhd_ctx *ctx, const void *u, const void *b, int where)
 MHD_API int mhd_get_state(mhd_ctx *ctx, void *u, void *b, int where);
 /* Device pointers of the current state (valid until the next mhd_step). */
 MHD_API int mhd_state_ptrs(mhd_ctx *ctx, void **u, void **b);
+/* device address of the step clock: 4 values of the state's precision (t, tf, dt, 1/c),
+ * written on the context stream by every step */
+MHD_API int mhd_clock_ptr(mhd_ctx *ctx, void **clock);
 
 /* nsteps full Strang steps x(F,A) T12 y(F,A) T13 z(F,A,A,F) T13 y(A,F) T12 x(A,F)
  * (C/mhd.c:59-124) with dt = cfl * calcfl, clamped so that t never passes tf

@@ -181,7 +181,7 @@ def test_correction_keeps_div_b_and_falls_back(clos, mhd, cuda):
     flags = torch.zeros(4, dtype=torch.int32, device="cuda")
     esum = torch.zeros(8, dtype=torch.float64, device="cuda")
     fb = torch.zeros(1, dtype=torch.int64, device="cuda")
-    args = (ut.data_ptr(), bt.data_ptr(), flags.data_ptr(), esum.data_ptr(), 1e-2, fb.data_ptr(), s)
+    args = (ut.data_ptr(), bt.data_ptr(), flags.data_ptr(), esum.data_ptr(), 1e-2, fb.data_ptr(), None, 0.0, s)
     assert L.mhd_cl_apply(ud.data_ptr(), bd.data_ptr(), od.data_ptr(), n, sd.data_ptr(), bscale, *args) == 0
     torch.cuda.synchronize()
     ur, br = co.apply_correction(u, b, out, n, osc, bscale)
