@@ -69,21 +69,25 @@ class Dataset:
         self.x = self.t = None
         self.stats = None
 
-    def finalize(self) -> cl.Stats:
-        """Channel statistics, then BF16 inputs [S][n^3][16] and targets [S][n^3][8]."""
+    def finalize(self, stats: "cl.Stats | None" = None) -> cl.Stats:
+        """Channel statistics (or the given ones: a net's own, to fine-tune it), then
+        BF16 inputs [S][n^3][16] and targets [S][n^3][8]."""
         torch = _torch()
         S, nv = self.count, self.n ** 3
         s = cl.stream_ptr()
-        sums = torch.zeros(16, dtype=torch.float64, device="cuda")
-        tsum = torch.zeros(16, dtype=torch.float64, device="cuda")
-        _check(cl.cl().mhd_cl_moments(self.raw_x.data_ptr(), 8, S * nv, sums.data_ptr(), s), "moments")
-        _check(cl.cl().mhd_cl_moments(self.raw_t.data_ptr(), 8, S * nv, tsum.data_ptr(), s), "moments")
-        sx, st = sums.cpu().numpy(), tsum.cpu().numpy()
-        cnt = float(S * nv)
-        mean = sx[:8] / cnt
-        std = np.sqrt(np.maximum(sx[8:] / cnt - mean ** 2, 1e-30))
-        trms = np.sqrt(np.maximum(st[8:] / cnt, 1e-30))
-        stats = cl.Stats(mean=mean, inv_std=1.0 / std, oscale=trms[:5], bscale=float(np.sqrt(np.mean(trms[5:] ** 2))))
+        if stats is None:
+            sums = torch.zeros(16, dtype=torch.float64, device="cuda")
+            tsum = torch.zeros(16, dtype=torch.float64, device="cuda")
+            _check(cl.cl().mhd_cl_moments(self.raw_x.data_ptr(), 8, S * nv, sums.data_ptr(), s), "moments")
+            _check(cl.cl().mhd_cl_moments(self.raw_t.data_ptr(), 8, S * nv, tsum.data_ptr(), s), "moments")
+            sx, st = sums.cpu().numpy(), tsum.cpu().numpy()
+            cnt = float(S * nv)
+            mean = sx[:8] / cnt
+            std = np.sqrt(np.maximum(sx[8:] / cnt - mean ** 2, 1e-30))
+            trms = np.sqrt(np.maximum(st[8:] / cnt, 1e-30))
+            stats = cl.Stats(mean=mean, inv_std=1.0 / std, oscale=trms[:5],
+                             bscale=float(np.sqrt(np.mean(trms[5:] ** 2))))
+        mean, std = np.asarray(stats.mean), 1.0 / np.asarray(stats.inv_std)
         self.x = torch.empty((S, nv * 16), dtype=torch.bfloat16, device="cuda")
         self.t = torch.empty((S, nv * 8), dtype=torch.bfloat16, device="cuda")
         f32 = dict(dtype=torch.float32, device="cuda")
@@ -156,6 +160,101 @@ def generate(runs: int, fine: int = 256, factor: int = 4, samples: int = 20, eve
     for c in (ctx_f, ctx_g, ctx_c):
         c.close()
     return ds
+
+
+def generate_onpolicy(net: cl.ClosureNet, runs: int, fine: int = 256, factor: int = 4, samples: int = 20,
+                      every: int = 45, seed0: int = 100, cfl: float = 0.7, gain: float = 1.0,
+                      base: "Dataset | None" = None, log=_log) -> Dataset:
+    """Pairs on the corrected trajectory (the states the net meets when it is
+    used): a coarse run corrected by `net` after every step follows each fine
+    run; at every sample time the input is the corrected coarse state and the
+    target is the filtered fine state one coarse step later minus a plain
+    coarse step from that input.  The raw pairs of `base` (if given, before
+    finalize) are kept in front."""
+    torch = _torch()
+    nc = fine // factor
+    old = base.count if base is not None else 0
+    ds = Dataset(old + runs * samples, nc)
+    if base is not None:
+        ds.raw_x[:old].copy_(base.raw_x[:old])
+        ds.raw_t[:old].copy_(base.raw_t[:old])
+        ds.count = old
+    L = cl.cl()
+    f32 = dict(dtype=torch.float32, device="cuda")
+    uf1, bf1 = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    ucs, bcs = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    uci, bci = torch.empty(nc ** 3 * 5, **f32), torch.empty(nc ** 3 * 3, **f32)
+    side = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    with Context(fine, fine, fine) as ctx_f, Context(fine, fine, fine) as ctx_g, Context(nc, nc, nc) as ctx_c, \
+            Context(nc, nc, nc) as ctx_p:
+        corr = cl.Corrector(net, nc, gain=gain)
+        for r in range(runs):
+            u, b = init_vortex(fine, fine, fine, seed=seed0 + r)
+            ctx_f.set_state(u, b)
+            du, db = torch.from_numpy(u).to("cuda"), torch.from_numpy(b).to("cuda")
+            _check(L.mhd_cl_filter(du.data_ptr(), db.data_ptr(), fine, factor, uci.data_ptr(), bci.data_ptr(),
+                                   cl.stream_ptr()), "filter")
+            torch.cuda.synchronize()
+            _set_state_dev(ctx_c, uci.data_ptr(), bci.data_ptr())
+            for q in range(samples):
+                if q:
+                    ctx_f.step(every, cfl=cfl)
+                tq = ctx_f.time()[0]
+                # the corrected coarse run, advanced to the fine run's time
+                if q:
+                    _run_to(ctx_c, tq / factor, cfl, 4, corrector=corr, stream=side, max_steps=100000)
+                ctx_c.sync()
+                cu, cb = ctx_c.state_ptrs()
+                _check(L.mhd_cl_features(cu, cb, nc, None, None, ds.raw_x[ds.count].data_ptr(), None,
+                                         cl.stream_ptr()), "features")
+                torch.cuda.synchronize()
+                # a plain coarse step from the corrected state
+                _set_state_dev(ctx_p, cu, cb)
+                ctx_p.step(1, cfl=cfl)
+                tc, _, _ = ctx_p.time()
+                _get_state_dev(ctx_p, ucs, bcs)
+                # the fine run one coarse step later, filtered
+                fu, fb = ctx_f.state_ptrs()
+                _set_state_dev(ctx_g, fu, fb)
+                ctx_g.set_time(0.0, tc * factor)
+                for _ in range(64):
+                    ctx_g.step(2, cfl=cfl)
+                    if reached(ctx_g.time()[0], tc * factor):
+                        break
+                gu, gb = ctx_g.state_ptrs()
+                s_ = cl.stream_ptr()
+                _check(L.mhd_cl_filter(gu, gb, fine, factor, uf1.data_ptr(), bf1.data_ptr(), s_), "filter")
+                _check(L.mhd_cl_diff(uf1.data_ptr(), bf1.data_ptr(), ucs.data_ptr(), bcs.data_ptr(), nc,
+                                     ds.raw_t[ds.count].data_ptr(), s_), "diff")
+                torch.cuda.synchronize()
+                ds.count += 1
+            if log and (r % max(1, runs // 8) == 0 or r == runs - 1):
+                log(f"generate_onpolicy: run {r + 1}/{runs}, {ds.count} samples, {time.perf_counter() - t0:.1f} s")
+    return ds
+
+
+def finetune(net: cl.ClosureNet, ds: Dataset, iters: int, batch: int = 4, lr: float = 3e-4, seed: int = 1,
+             log=_log):
+    """More AdamW iterations of an existing net on a finalized dataset (its stats kept)."""
+    torch = _torch()
+    n, S = ds.n, ds.count
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xb = torch.empty((batch, n ** 3 * 16), dtype=torch.bfloat16, device="cuda")
+    tb = torch.empty((batch, n ** 3 * 8), dtype=torch.bfloat16, device="cuda")
+    t0 = time.perf_counter()
+    for it in range(iters):
+        idx = torch.from_numpy(rng.integers(0, S, size=batch)).to("cuda")
+        torch.index_select(ds.x, 0, idx, out=xb)
+        torch.index_select(ds.t, 0, idx, out=tb)
+        a = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * it / iters)))
+        net.forward(xb, batch, n)
+        net.loss(tb, batch, n)
+        net.backward(xb, batch, n)
+        net.adamw(a)
+        if log and (it % max(1, iters // 10) == 0 or it == iters - 1):
+            log(f"finetune: iter {it} loss {net.loss_value():.4f} ({time.perf_counter() - t0:.1f} s)")
+    return net
 
 
 def train(ds: Dataset, iters: int = 3000, batch: int = 4, lr: float = 1e-3, seed: int = 0, val_frac: float = 0.05,
@@ -373,11 +472,26 @@ def main(argv=None):
     ap.add_argument("--crossings", type=float, nargs="+", default=[0.5, 1.0, 2.0])
     ap.add_argument("--gain", type=float, default=1.0, help="scale of the applied correction")
     ap.add_argument("--model", default="closure_model.npz")
-    ap.add_argument("--load", default=None, help="skip data and training, evaluate this model")
+    ap.add_argument("--load", default=None, help="start from this model (evaluate it, or fine-tune it)")
+    ap.add_argument("--onpolicy", type=int, default=0,
+                    help="with --load: fine-tune on pairs from this many corrected runs (plus --runs filtered ones)")
     ap.add_argument("--report", default="closure_report.json")
     a = ap.parse_args(argv)
     report = {"args": vars(a)}
-    if a.load:
+    if a.load and a.onpolicy:
+        net = cl.ClosureNet.load(a.load)
+        t0 = time.perf_counter()
+        base = generate(a.runs, a.fine, a.factor, a.samples, a.every) if a.runs else None
+        ds = generate_onpolicy(net, a.onpolicy, a.fine, a.factor, a.samples, a.every, base=base)
+        del base
+        ds.finalize(stats=net.stats)
+        report["generate_s"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        finetune(net, ds, a.iters, lr=a.lr)
+        report["train_s"] = time.perf_counter() - t0
+        net.save(a.model)
+        del ds
+    elif a.load:
         net = cl.ClosureNet.load(a.load)
     else:
         t0 = time.perf_counter()
