@@ -404,6 +404,10 @@ def ncu_case(args):
 
     n = args.size
     u0, b0 = mhd.init_turbulence(n, seed=0)
+    for kv in args.knob:
+        key, val = kv.split("=")
+        if mhd.lib().mhd_tune_set(key.encode(), int(val)) != 0:
+            raise SystemExit(f"bad knob {kv}")
     with mhd.Context(n, n, n) as ctx:
         ctx.use_graphs(False)
         ctx.set_state(u0, b0)
@@ -426,6 +430,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error leg")
     ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure leg")
     ap.add_argument("--ncu-case", action="store_true", help="run the short profiling case only")
+    ap.add_argument("--knob", action="append", default=[], help="launch-shape knob key=value for --ncu-case")
     ap.add_argument("--fp64-steps", type=int, default=100, help="steps of the FP64 error leg")
     args = ap.parse_args()
     if args.warmup < 3:

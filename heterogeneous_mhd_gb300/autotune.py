@@ -21,7 +21,8 @@ from pathlib import Path
 from . import Context, init_turbulence, lib
 
 CACHE = Path(os.environ.get("MHD_GB300_TUNE_CACHE", Path(__file__).resolve().parent / "lib" / "tuning.json"))
-KNOBS = ("fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K", "fluidx.cells")
+KNOBS = ("fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K", "fluidx.cells", "advect.kernel",
+         "advect.xk")
 
 
 def set_knob(key: str, value: int) -> None:
@@ -67,6 +68,11 @@ def candidates(n: int):
     if n % 8 == 0 and 8 <= n // 8 <= 64 and (n // 8) & (n // 8 - 1) == 0:
         fx += [{"fluidx.threads": t, "fluidx.cells": 8} for t in (32, 64, 128, 256) if t >= n // 8]
     adv = []
+    if n % 4 == 0 and n % 32 == 0:  # the x-walking kernel
+        for xk in (2, 4, 8):
+            for slots in (2, 3):
+                if n % xk == 0:
+                    adv.append({"advect.kernel": 4, "advect.xk": xk, "advect.slots": slots})
     for cells in (4, 8):
         t = n // cells
         if n % cells or t < 4 or t > 128 or (t & (t - 1)):
@@ -77,7 +83,8 @@ def candidates(n: int):
                     continue
                 for k in (4, 8, 16, 32):
                     if n % k == 0:
-                        adv.append({"advect.cells": cells, "advect.slots": slots, "advect.J": j, "advect.K": k})
+                        adv.append({"advect.kernel": 3, "advect.cells": cells, "advect.slots": slots,
+                                    "advect.J": j, "advect.K": k})
     return fx, adv
 
 

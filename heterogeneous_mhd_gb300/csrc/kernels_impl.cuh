@@ -7,6 +7,7 @@
 // a general kernel for every other shape.  FP64 uses the general kernels.
 #include "mhd_advect2.cuh"
 #include "mhd_advect3.cuh"
+#include "mhd_advect4.cuh"
 #include "mhd_fluidx2.cuh"
 #include "mhd_launch.h"
 #include "mhd_transpose2.cuh"
@@ -292,6 +293,80 @@ static cudaError_t advect_sweep(const AdvectArgs& a, const A3Plan& p3, cudaStrea
     return (p3.NS == 2) ? launch_ad3_t<8, 2, AX>(a, p3.T, s) : launch_ad3_t<8, 3, AX>(a, p3.T, s);
 }
 
+// x-walking kernel (FP32, the x sweep), chosen by the knob advect.kernel = 4
+// (the autotuner tries it; the marching kernel measured faster on GB300 at
+// 256^3, so it is not the planner's default): KT planes per CTA (4 by
+// default, or advect.xk), NS chunk buffers (2, or 3 by advect.slots); nx a
+// multiple of 4 and ny a multiple of 32.
+struct A4Plan {
+    int KT, NS;
+};
+
+static bool plan_advect4(const AdvectArgs& a, bool aligned, A4Plan& p)
+{
+    const int kn = tune_value(TUNE_ADVECT_KERNEL);
+    if (!kV2 || !aligned || a.axis != 0 || kn != 4)
+        return false;
+    if (a.nx % kA4X != 0 || a.ny % kA4J != 0)
+        return false;
+    if ((long long)a.nx * a.ny * a.nz * 5 >= (1LL << 31))  // 32-bit offsets inside a box
+        return false;
+    const int kt = tune_value(TUNE_ADVECT_XK);
+    p.NS = tune_value(TUNE_ADVECT_SLOTS) == 3 ? 3 : 2;
+    p.KT = 0;
+    for (int k : {4, 8, 2})
+        if (!p.KT && (kt == 0 || kt == k) && a.nz % k == 0)
+            p.KT = k;
+    return p.KT != 0;
+}
+
+// Persistent grid: the CTAs that fit on the device at once, shared among the
+// boxes of the launch, each with at least 8 chunks of work.
+template <int KT, int NS>
+static cudaError_t launch_ad4(const AdvectArgs& a, cudaStream_t s)
+{
+    static bool attr = false;
+    static int per_sm = 0, nsm = 0;
+    cudaError_t e = allow_smem(k_advect4<EX, KT, NS>, attr, true);
+    if (e != cudaSuccess)
+        return e;
+    const size_t smem = advect4_smem_bytes(KT, NS);
+    if (!per_sm) {
+        int dev = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess)
+            e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect4<EX, KT, NS>, advect4_threads(KT),
+                                                              smem);
+        if (e != cudaSuccess)
+            return e;
+        if (per_sm < 1)
+            return cudaErrorInvalidConfiguration;
+    }
+    const long long work = (long long)(a.ny / kA4J) * (a.nz / KT) * (a.nx / kA4X);
+    long long ctas = ((long long)per_sm * nsm + a.bs.count - 1) / a.bs.count;
+    const long long cap = (work / 8 > 0) ? work / 8 : 1;
+    if (ctas > cap)
+        ctas = cap;
+    dim3 grid((unsigned)ctas, 1, a.bs.count);
+    k_advect4<EX, KT, NS><<<grid, advect4_threads(KT), smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+static cudaError_t advect_x4(const AdvectArgs& a, const A4Plan& p, cudaStream_t s)
+{
+    switch (p.KT * 10 + p.NS) {
+    case 82: return launch_ad4<8, 2>(a, s);
+    case 83: return launch_ad4<8, 3>(a, s);
+    case 42: return launch_ad4<4, 2>(a, s);
+    case 43: return launch_ad4<4, 3>(a, s);
+    case 22: return launch_ad4<2, 2>(a, s);
+    case 23: return launch_ad4<2, 3>(a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
 template <int C, int T>
 static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
 {
@@ -319,6 +394,9 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
     const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
                          reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
     if constexpr (kV2) {
+        A4Plan p4;
+        if (plan_advect4(a, (al & 15) == 0, p4))
+            return advect_x4(a, p4, s);
         A3Plan p3;
         if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3)) {
             a.P = p3.J;

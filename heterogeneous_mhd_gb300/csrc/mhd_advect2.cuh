@@ -68,6 +68,116 @@ __device__ __forceinline__ void stg_chunk(R* dst, const R (&src)[NF])
     }
 }
 
+// Per-cell steps of tvdb, shared by every advectbyzx kernel.  EXACT: the
+// reference's expressions (compiled without contraction).  FAST: every
+// rounding is explicit (__fadd_rn, __fmul_rn and __fmaf_rn are never
+// contracted), so all kernels compute the same bits whatever the compiler
+// does around the calls.
+__device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double r_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double r_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double r_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float r_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double r_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// Raw face velocity (C/advectbyzxA1.c:34, C/advectbyzxB1.c:34) from m_x and
+// rho of the pencil below (m) and the current one (c).
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_face(R mm, R mc, R rm, R rc)
+{
+    if constexpr (EX)
+        return (mm + mc) / (rm + rc);
+    else
+        return fast_div(r_add(mm, mc), r_add(rm, rc));
+}
+
+// 1-2-1 smoothing of the face velocity (C/advectbyzxA1.c:36-41): vm, v, vp at i-1, i, i+1.
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_smooth(R vm, R v, R vp)
+{
+    using W = wide_t<R, EX>;
+    if constexpr (EX)
+        return R((W(vm + vp) + W(2.0) * W(v)) / W(4.0));
+    else
+        return r_mul(r_fma(R(2), v, r_add(vm, vp)), R(0.25));
+}
+
+// b vg (C/tvdb.c:31-34), vg b1 (C/tvdb.c:55-60)
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_prod(R x, R y)
+{
+    if constexpr (EX)
+        return x * y;
+    else
+        return r_mul(x, y);
+}
+
+// vh = (vg(i) + vg(i+1)) / 2 in the abXYc form (C/tvdb.c:25-29)
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_vh(R vg, R vgn)
+{
+    if constexpr (EX)
+        return lin<R, EX>(R(0.5), vg, R(0.5), vgn);
+    else
+        return r_fma(R(0.5), vg, r_mul(R(0.5), vgn));
+}
+
+// Half step b1 = b - (f1(i) - f1(i-1)) dt / 2 (C/tvdb.c:41-47).
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_half(R bv, R f1, R fm, R dt)
+{
+    using W = wide_t<R, EX>;
+    if constexpr (EX)
+        return R(W(bv) - W((f1 - fm) * dt) / W(2.0));
+    else  // dt / 2 is loop-invariant: one fused multiply-add per cell
+        return r_fma(r_sub(fm, f1), r_mul(dt, R(0.5)), bv);
+}
+
+// Limited upwind flux times dt at i+1/2 (C/tvdb.c:54-78) from vb = vg b1 at
+// i-1, i, i+1, i+2 and the sign of vh(i).
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_flux(R vbm, R vb0, R vbp, R vbpp, R vh, R dt)
+{
+    if constexpr (EX) {
+        using W = wide_t<R, EX>;
+        R w, wp, wm;
+        if (vh > R(0)) {
+            w = vb0;
+            wp = R(W(vbp - w) / W(2.0));
+            wm = R(W(w - vbm) / W(2.0));
+        } else {
+            w = vbp;
+            wp = R(W(w - vbpp) / W(2.0));
+            wm = R(W(vb0 - w) / W(2.0));
+        }
+        const R dw = vanleer<R, EX>(wm, wp);
+        return (w + dw) * dt;
+    } else {
+        // The same differences with the operands selected (no branch), and the
+        // limiter on the undivided differences: with wm = dm/2, wp = dp/2,
+        // 2 wm wp / (wm + wp) = dm dp / (dm + dp).
+        const bool up = vh > R(0);
+        const R w = up ? vb0 : vbp;
+        const R dp = r_sub(vbp, up ? vb0 : vbpp);
+        const R dm = r_sub(vb0, up ? vbm : vbp);
+        const R p = r_mul(dm, dp);
+        const R dw = (p > R(0)) ? fast_div(p, r_add(dm, dp)) : R(0);
+        return r_mul(r_add(w, dw), dt);
+    }
+}
+
+// Advected field b - (flux(i) - flux(i-1)) (C/tvdb.c:79-88)
+template <typename R, bool EX>
+__device__ __forceinline__ R tvdb_new(R bv, R flux, R fm)
+{
+    if constexpr (EX)
+        return bv - (flux - fm);
+    else
+        return r_sub(bv, r_sub(flux, fm));
+}
+
 // One tvdb row held by T threads with C cells each: from the raw face
 // velocity vr (C/advectbyzxA1.c:31-35) and the advected field bv, the 1-2-1
 // smoothing (C/advectbyzxA1.c:36-41) and tvdb (C/tvdb.c:10-91).  Returns
@@ -77,7 +187,6 @@ template <typename R, bool EX, int C, int T, bool NM>
 __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)[C], const R (&bv)[C], R dt, R* seam,
                                          R (&F)[C], R (&bnew)[C])
 {
-    using W = wide_t<R, EX>;
     // ---- 1-2-1 smoothing (C/advectbyzxA1.c:36-41)
     R vg[C];
     {
@@ -88,10 +197,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
         for (int m = 0; m < C; m++) {
             const R vm = (m > 0) ? vr[m - 1] : l[0];
             const R vp = (m + 1 < C) ? vr[m + 1] : rr[0];
-            if constexpr (EX)
-                vg[m] = R((W(vm + vp) + W(2.0) * W(vr[m])) / W(4.0));
-            else
-                vg[m] = ((vm + vp) + R(2) * vr[m]) * R(0.25);
+            vg[m] = tvdb_smooth<R, EX>(vm, vr[m], vp);
         }
     }
     // ---- tvdb half step (C/tvdb.c:25-52)
@@ -100,7 +206,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
         R t2[C];
 #pragma unroll
         for (int m = 0; m < C; m++)
-            t2[m] = bv[m] * vg[m];
+            t2[m] = tvdb_prod<R, EX>(bv[m], vg[m]);
         R xs[2] = {vg[0], t2[0]}, xr[2];
         g.template shift<2>(xs, xr, +1, seam, 0);
         R f1[C];
@@ -108,7 +214,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
         for (int m = 0; m < C; m++) {
             const R vgn = (m + 1 < C) ? vg[m + 1] : xr[0];
             const R t2n = (m + 1 < C) ? t2[m + 1] : xr[1];
-            vh[m] = lin<R, EX>(R(0.5), vg[m], R(0.5), vgn);
+            vh[m] = tvdb_vh<R, EX>(vg[m], vgn);
             f1[m] = (vh[m] > R(0)) ? t2[m] : t2n;
         }
         R fl[1], fx[1] = {f1[C - 1]};
@@ -116,10 +222,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
 #pragma unroll
         for (int m = 0; m < C; m++) {
             const R fm = (m > 0) ? f1[m - 1] : fl[0];
-            if constexpr (EX)
-                b1[m] = R(W(bv[m]) - W((f1[m] - fm) * dt) / W(2.0));
-            else
-                b1[m] = bv[m] - (f1[m] - fm) * dt * R(0.5);
+            b1[m] = tvdb_half<R, EX>(bv[m], f1[m], fm, dt);
         }
     }
     // ---- limited upwind flux (C/tvdb.c:54-78)
@@ -128,7 +231,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
         R vb[C];
 #pragma unroll
         for (int m = 0; m < C; m++)
-            vb[m] = vg[m] * b1[m];
+            vb[m] = tvdb_prod<R, EX>(vg[m], b1[m]);
         R l[1], x0[1] = {vb[C - 1]};
         g.template shift<1>(x0, l, -1, seam, 0);
         R xs[2] = {vb[0], vb[1 < C ? 1 : 0]}, xr[2];
@@ -139,25 +242,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
             const R vbm = (m > 0) ? vb[m - 1] : l[0];
             const R vbp = (m + 1 < C) ? vb[m + 1] : xr[0];
             const R vbpp = (m + 2 < C) ? vb[m + 2] : ((m + 2 == C) ? xr[0] : xr[1]);
-            R w, wp, wm;
-            if constexpr (EX) {
-                if (vh[m] > R(0)) {
-                    w = vb[m];
-                    wp = R(W(vbp - w) / W(2.0));
-                    wm = R(W(w - vbm) / W(2.0));
-                } else {
-                    w = vbp;
-                    wp = R(W(w - vbpp) / W(2.0));
-                    wm = R(W(vb[m] - w) / W(2.0));
-                }
-            } else {  // the same differences with the operands selected: no branch
-                const bool up = vh[m] > R(0);
-                w = up ? vb[m] : vbp;
-                wp = (vbp - (up ? vb[m] : vbpp)) * R(0.5);
-                wm = (vb[m] - (up ? vbm : vbp)) * R(0.5);
-            }
-            const R dw = vanleer<R, EX>(wm, wp);
-            flux[m] = (w + dw) * dt;
+            flux[m] = tvdb_flux<R, EX>(vbm, vb[m], vbp, vbpp, vh[m], dt);
         }
     }
     // ---- b - (flux - flux(i-1)) (C/tvdb.c:79-88) and F(i) = flux(i-1)
@@ -167,7 +252,7 @@ __device__ __forceinline__ void tvdb_row(const Group<R, T, NM>& g, const R (&vr)
 #pragma unroll
         for (int m = 0; m < C; m++) {
             F[m] = (m > 0) ? flux[m - 1] : l[0];
-            bnew[m] = bv[m] - (flux[m] - F[m]);
+            bnew[m] = tvdb_new<R, EX>(bv[m], flux[m], F[m]);
         }
     }
 }

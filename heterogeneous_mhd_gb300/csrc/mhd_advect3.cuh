@@ -144,11 +144,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     auto face_v = [&](const float (&um)[C * 5], const float (&uc)[C * 5], float (&vr)[C]) {
 #pragma unroll
         for (int m = 0; m < C; m++) {
-            const float num = um[5 * m + UM] + uc[5 * m + UM], den = um[5 * m] + uc[5 * m];
-            if constexpr (EX)
-                vr[m] = num / den;
-            else
-                vr[m] = fast_div(num, den);
+            vr[m] = tvdb_face<float, EX>(um[5 * m + UM], uc[5 * m + UM], um[5 * m], uc[5 * m]);
         }
     };
 

@@ -45,6 +45,8 @@ enum TuneKey : int {
     TUNE_ADVECT_J,            // pencils per CTA along j
     TUNE_ADVECT_K,            // planes per CTA along k
     TUNE_FLUIDX_C,            // cells per thread of the register-resident fluidx (4, or 8: one warp per pencil)
+    TUNE_ADVECT_KERNEL,       // advectbyzx of the x sweep: 3 marching along k, 4 walking along x
+    TUNE_ADVECT_XK,           // planes per CTA of the x-walking advectbyzx (2, 4 or 8)
     TUNE_COUNT
 };
 int tune_value(int key);

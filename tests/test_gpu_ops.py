@@ -106,6 +106,49 @@ def test_exact_ops_bitwise_vs_oracle(shape, mhd, cuda, oracle32):
         assert rel_l2(out[name], ref[name]) < FAST_OP_TOL, f"{name} {shape}"
 
 
+# x-walking advectbyzx: one chunk per pencil (nx = 4), a single j tile (its
+# halo pencils are its own, periodic), an odd number of chunks, several tiles
+X4_SHAPES = [(4, 32, 2), (8, 32, 4), (36, 64, 8), (32, 32, 6), (128, 96, 12), (64, 32, 16)]
+X4_PLANS = [(2, 2), (2, 3), (4, 2), (4, 3), (8, 2), (8, 3)]  # (planes per CTA, chunk buffers)
+
+
+@pytest.mark.parametrize("shape", X4_SHAPES)
+def test_x_walking_advect_vs_oracle(shape, mhd, cuda, oracle32):
+    """The x-walking advectbyzx forced on every planes-per-CTA / ring-depth
+    choice that divides nz: EXACT bit for bit against the oracle, FAST within
+    the operator tolerance."""
+    from heterogeneous_mhd_gb300 import autotune
+    torch = cuda
+    nx, ny, nz = shape
+    rng = np.random.default_rng(nx * 31 + nz)
+    u, b = mhd.init_vortex(nx, ny, nz, seed=int(rng.integers(1 << 20)))
+    u = (u * (1 + 0.05 * rng.standard_normal(u.shape))).astype(np.float32)
+    b = (b + 0.05 * rng.standard_normal(b.shape)).astype(np.float32)
+    bin_ = (b * np.float32(0.75)).astype(np.float32)
+    ref = bin_.copy()
+    oracle32.advectbyzx(u.copy(), ref, nx, ny, nz, DT, u.copy(), b.copy())
+    tried = 0
+    try:
+        for kt, ns in X4_PLANS:
+            if nz % kt:
+                continue
+            autotune.apply({"advect.kernel": 4, "advect.xk": kt, "advect.slots": ns})
+            for exact in (True, False):
+                with mhd.Context(1, 1, 1, exact=exact) as ctx:
+                    bo = dev(torch, bin_)
+                    ctx.op_advectbyzx(bo, dev(torch, u), dev(torch, b), nx, ny, nz, DT)
+                    ctx.sync()
+                    got = host(bo)
+                if exact:
+                    assert bitwise_equal(got, ref), f"{shape} KT={kt} NS={ns}"
+                else:
+                    assert rel_l2(got, ref) < FAST_OP_TOL, f"{shape} KT={kt} NS={ns}"
+            tried += 1
+    finally:
+        autotune.apply({})
+    assert tried > 0
+
+
 def test_in_place_and_aliased_arguments(mhd, cuda, oracle32):
     """The reference's C/ allows u == update_u for fluidx and b == update_b for
     advectbyzx and the transposes (it works pencil by pencil / plane by plane);

@@ -186,7 +186,9 @@ def test_full_size_512_properties(mhd, cuda):
 
 
 @pytest.mark.parametrize("knobs", [{"fluidx.cells": 8, "fluidx.threads": 32}, {"fluidx.cells": 8, "fluidx.threads": 64},
-                                   {"advect.cells": 8}])
+                                   {"advect.kernel": 3}, {"advect.kernel": 3, "advect.cells": 8},
+                                   {"advect.kernel": 4, "advect.xk": 2, "advect.slots": 2},
+                                   {"advect.kernel": 4, "advect.xk": 4}])
 def test_launch_shapes_do_not_change_results(knobs, mhd, cuda):
     """Every launch shape the tuner may pick computes the same numbers: the
     EXACT kernels reproduce the reference checksums of the 64^3 vortex and the
@@ -204,3 +206,20 @@ def test_launch_shapes_do_not_change_results(knobs, mhd, cuda):
         assert bitwise_equal(uf, ref_fast[0]) and bitwise_equal(bf, ref_fast[1])
     finally:
         autotune.apply({k: 0 for k in knobs})
+
+
+@pytest.mark.parametrize("kt,ns", [(2, 2), (4, 3), (8, 2), (8, 3)])
+def test_x_walking_advect_step_exact(kt, ns, mhd, cuda, oracle32):
+    """Strang steps with the x-walking advectbyzx forced (the step reads b(1)
+    from update_b, the staged form): EXACT bit for bit against the oracle on a
+    box whose three sweeps have different pencil lengths and tile counts."""
+    from heterogeneous_mhd_gb300 import autotune
+    shape = (32, 64, 64)
+    u0, b0 = mhd.init_vortex(*shape, seed=3)
+    ref = oracle32.strang(u0, b0, *shape, 2)
+    try:
+        autotune.apply({"advect.kernel": 4, "advect.xk": kt, "advect.slots": ns})
+        u, b, _ = run(mhd, u0, b0, shape, 2, exact=True)
+    finally:
+        autotune.apply({})
+    assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1])
