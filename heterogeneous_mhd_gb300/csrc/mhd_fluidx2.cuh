@@ -129,11 +129,16 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
         const R b1next = bj[3 * inext + B0];
 #pragma unroll
         for (int m = 0; m < C; m++) {
-            const R h0 = R(0.5) * bjf[3 * m + B0];
-            const R h0p = R(0.5) * ((m + 1 < C) ? bjf[3 * (m + 1) + B0] : b1next);
-            f[m][0] = h0 + h0p;
-            f[m][1] = R(0.5) * bjf[3 * m + B1] + bpf[3 * m + B1] / R(2);
-            f[m][2] = R(0.5) * bjf[3 * m + B2] + bkf[3 * m + B2] / R(2);
+            const R b0n = (m + 1 < C) ? bjf[3 * (m + 1) + B0] : b1next;
+            if constexpr (EX) {
+                f[m][0] = R(0.5) * bjf[3 * m + B0] + R(0.5) * b0n;
+                f[m][1] = R(0.5) * bjf[3 * m + B1] + bpf[3 * m + B1] / R(2);
+                f[m][2] = R(0.5) * bjf[3 * m + B2] + bkf[3 * m + B2] / R(2);
+            } else {  // the same values: halving is exact
+                f[m][0] = R(0.5) * (bjf[3 * m + B0] + b0n);
+                f[m][1] = R(0.5) * (bjf[3 * m + B1] + bpf[3 * m + B1]);
+                f[m][2] = R(0.5) * (bjf[3 * m + B2] + bkf[3 * m + B2]);
+            }
         }
     };
     R q[C][5], f[C][3];
@@ -227,13 +232,21 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
         R frp[5], gln[5];
         g.template shift<5>(fr[C - 1], frp, -1, seam, 0);
         g.template shift<5>(gl[0], gln, +1, seam, 1);
-        R dm[C][5], dl[C][5];  // dfrm(i), dflm(i)
+        // dfrm(i), dflm(i); FAST keeps them undivided (2 dfrm, 2 dflm: the halves
+        // are exact, and the limiter below absorbs the factor)
+        R dm[C][5], dl[C][5];
 #pragma unroll
         for (int m = 0; m < C; m++)
 #pragma unroll
             for (int s = 0; s < 5; s++) {
-                dm[m][s] = lin<R, EX>(R(0.5), fr[m][s], R(-0.5), (m > 0) ? fr[m - 1][s] : frp[s]);
-                dl[m][s] = lin<R, EX>(R(0.5), gl[m][s], R(-0.5), (m + 1 < C) ? gl[m + 1][s] : gln[s]);
+                const R frm = (m > 0) ? fr[m - 1][s] : frp[s], gln1 = (m + 1 < C) ? gl[m + 1][s] : gln[s];
+                if constexpr (EX) {
+                    dm[m][s] = lin<R, EX>(R(0.5), fr[m][s], R(-0.5), frm);
+                    dl[m][s] = lin<R, EX>(R(0.5), gl[m][s], R(-0.5), gln1);
+                } else {
+                    dm[m][s] = fr[m][s] - frm;
+                    dl[m][s] = gl[m][s] - gln1;
+                }
             }
 #pragma unroll
         for (int s = 0; s < 5; s++) {
@@ -252,9 +265,11 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
                     dfr = vanleer<R, EX>(dmn, dm[m][s]);
                     dfl = vanleer<R, EX>(dln, dl[m][s]);
                 } else {
-                    // branch-free: the quotient is computed for every cell and selected
+                    // branch-free: the quotient is computed for every cell and selected.
+                    // With a = A/2, b = B/2: 2ab / (a + b) = AB / (A + B), and every
+                    // factor dropped is a power of two, so the value is the halved form's.
                     const R pr = dmn * dm[m][s], pl = dln * dl[m][s];
-                    const R qr = fast_div(R(2) * pr, dmn + dm[m][s]), ql = fast_div(R(2) * pl, dln + dl[m][s]);
+                    const R qr = fast_div(pr, dmn + dm[m][s]), ql = fast_div(pl, dln + dl[m][s]);
                     dfr = (pr > R(0)) ? qr : R(0);
                     dfl = (pl > R(0)) ? ql : R(0);
                 }
