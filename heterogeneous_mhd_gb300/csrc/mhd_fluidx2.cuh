@@ -178,16 +178,23 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
     }
     R u1[C][5];
     {
+        // FAST keeps the flux undivided (2 flux: the half is exact) and puts the
+        // factor into the step: q + (hdt/2)(F(i) - F(i-1)) is the same value.
         R gnext[5], flux[C][5];
         g.template shift<5>(gl[0], gnext, +1, seam, 0);
 #pragma unroll
         for (int m = 0; m < C; m++)
 #pragma unroll
-            for (int s = 0; s < 5; s++)
-                flux[m][s] = lin<R, EX>(R(0.5), fr[m][s], R(-0.5), (m + 1 < C) ? gl[m + 1][s] : gnext[s]);
+            for (int s = 0; s < 5; s++) {
+                const R gn = (m + 1 < C) ? gl[m + 1][s] : gnext[s];
+                if constexpr (EX)
+                    flux[m][s] = lin<R, EX>(R(0.5), fr[m][s], R(-0.5), gn);
+                else
+                    flux[m][s] = fr[m][s] - gn;
+            }
         R fprev[5];
         g.template shift<5>(flux[C - 1], fprev, -1, seam, 1);
-        const R hdt = R(W(-1.0) * W(dt) / W(2.0));
+        const R hdt = EX ? R(W(-1.0) * W(dt) / W(2.0)) : R(-0.25) * dt;
 #pragma unroll
         for (int m = 0; m < C; m++)
 #pragma unroll
@@ -274,14 +281,17 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
                     dfl = (pl > R(0)) ? ql : R(0);
                 }
                 const R gn = (m + 1 < C) ? gl[m + 1][s] : gln[s];
-                flux[m][s] = lin<R, EX>(R(0.5), lin<R, EX>(R(1), fr[m][s], R(-1), gn), R(0.5),
-                                        lin<R, EX>(R(1), dfr, R(-1), dfl));
+                if constexpr (EX)
+                    flux[m][s] = lin<R, EX>(R(0.5), lin<R, EX>(R(1), fr[m][s], R(-1), gn), R(0.5),
+                                            lin<R, EX>(R(1), dfr, R(-1), dfl));
+                else  // undivided (2 flux), the half goes into the step below
+                    flux[m][s] = (fr[m][s] - gn) + (dfr - dfl);
             }
     }
     {
         R fprev[5];
         g.template shift<5>(flux[C - 1], fprev, -1, seam, 1);
-        const R mdt = R(W(-1.0) * W(dt));
+        const R mdt = EX ? R(W(-1.0) * W(dt)) : R(-0.5) * dt;
         R of[C * 5];
         load_q(q);
 #pragma unroll
