@@ -162,8 +162,11 @@ MHD_API long long mhd_launch_count(mhd_ctx *ctx);
  * (heterogeneous_mhd_gb300/autotune.py).  Keys: "fluidx.threads" (threads
  * per CTA of the register-resident fluidx: 64, 128 or 256), "advect.cells"
  * (cells per thread of the marching advectbyzx: 4 or 8), "advect.slots"
- * (plane-slab ring depth: 2 or 3), "advect.J" (pencils per CTA), "advect.K"
- * (planes per CTA).  0 restores the planner's own choice; a value that does
+ * (plane-slab ring depth: 2 or 3; chunk buffers of the x-walking kernel),
+ * "advect.J" (pencils per CTA), "advect.K" (planes per CTA), "fluidx.cells"
+ * (4, or 8: one warp per pencil), "advect.kernel" (3: the marching
+ * advectbyzx, 4: the x-walking one) and "advect.xk" (planes per CTA of the
+ * x-walking kernel: 2, 4 or 8).  0 restores the planner's own choice; a value that does
  * not fit the grid is ignored.  Captured step graphs are rebuilt on the next
  * mhd_step.  mhd_tune_get returns the current value (-1 for an unknown key). */
 MHD_API int mhd_tune_set(const char *key, int value);
