@@ -114,3 +114,26 @@ def test_batch_device_buffers(mhd, cuda):
         torch.cuda.synchronize()
         hu, hb = bt.get_box(0)
         assert bitwise_equal(ou.cpu().numpy(), hu) and bitwise_equal(ob.cpu().numpy(), hb)
+
+
+def test_batch_x_walking_advect_exact_vs_oracle(mhd, cuda, oracle32):
+    """Batched classes with the x-walking advectbyzx forced: several boxes of
+    one class in one launch (the persistent CTAs of each box find it by
+    blockIdx.z); EXACT bit for bit against the oracle."""
+    from heterogeneous_mhd_gb300 import autotune
+    cfg = mhd.batch_config(4, seed=13)
+    for x, n in zip(cfg, (32, 64, 32, 64)):
+        x["n"] = n
+    try:
+        autotune.apply({"advect.kernel": 4, "advect.xk": 4})
+        bt, ics = make_batch(mhd, cfg, exact=True)
+        with bt:
+            bt.step(3)
+            bt.sync()
+            for i, box in enumerate(cfg):
+                n = box["n"]
+                u, b = bt.get_box(i)
+                ou, ob, _, _, _ = oracle32.strang(*ics[i], n, n, n, 3, 0.7)
+                assert bitwise_equal(u, ou) and bitwise_equal(b, ob), (i, box)
+    finally:
+        autotune.apply({})
