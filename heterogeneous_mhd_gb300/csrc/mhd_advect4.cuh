@@ -161,7 +161,8 @@ __device__ __forceinline__ void a4_face(const float (&rm)[4], const float (&mm)[
         vx[m] = tvdb_face<float, EX>(mm[m], mc[m], rm[m], rc[m]);
 }
 
-// CTAs per SM the register budget is sized for (shared memory allows as many)
+// CTAs per SM the register budget is sized for (shared memory allows as many,
+// except KT = 2 with three buffers: 4)
 __host__ __device__ constexpr int advect4_min_ctas(int KT, int NS)
 {
     return KT == 2 ? 5 : (KT == 4 ? 3 : 1);
