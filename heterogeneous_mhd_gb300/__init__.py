@@ -28,6 +28,7 @@ __all__ = [
 ]
 
 MHD_OK = 0
+MHD_ERR_ARG, MHD_ERR_CUDA, MHD_ERR_TIMEOUT, MHD_ERR_NONFINITE, MHD_ERR_UNSUPPORTED, MHD_ERR_NOMEM = 1, 2, 3, 4, 5, 6
 MHD_F32, MHD_F64 = 0, 1
 MHD_MODE_FAST, MHD_MODE_EXACT = 0, 2
 MHD_HOST, MHD_DEVICE = 0, 1
@@ -93,6 +94,8 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
                                    C.POINTER(C.c_longlong)]),
         "mhd_use_graphs": (C.c_int, [_vp, C.c_int]),
         "mhd_check": (C.c_int, [_vp]),
+        "mhd_clear_errors": (C.c_int, [_vp]),
+        "mhd_selftest_wait": (C.c_int, [_vp, C.c_double]),
         "mhd_profile": (C.c_int, [_vp, C.c_int]),
         "mhd_profile_read": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
         "mhd_profile_reset": (C.c_int, [_vp]),
@@ -301,6 +304,14 @@ class Context:
 
     def check(self) -> int:
         return lib().mhd_check(self._h)
+
+    def clear_errors(self) -> None:
+        _check(lib().mhd_clear_errors(self._h), "mhd_clear_errors")
+
+    def selftest_wait(self, seconds: float = 0.01) -> None:
+        """Queue a kernel whose bounded wait runs out after `seconds`: the next
+        check() returns MHD_ERR_TIMEOUT and the context stays usable."""
+        _check(lib().mhd_selftest_wait(self._h, float(seconds)), "mhd_selftest_wait")
 
     def use_graphs(self, on: bool) -> None:
         _check(lib().mhd_use_graphs(self._h, 1 if on else 0), "mhd_use_graphs")

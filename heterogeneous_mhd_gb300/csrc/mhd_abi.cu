@@ -802,6 +802,42 @@ extern "C" MHD_API int mhd_check(mhd_ctx* c)
     return set_err(MHD_OK);
 }
 
+extern "C" MHD_API int mhd_clear_errors(mhd_ctx* c)
+{
+    if (!c)
+        return set_err(MHD_ERR_ARG);
+    if (cudaMemsetAsync(c->err_dev, 0, sizeof(int), c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    return set_err(MHD_OK);
+}
+
+// Self-test of the bounded waits: one warp waits on an mbarrier that expects
+// one arrival which nothing makes.  After `limit` SM cycles the wait gives up,
+// the kernel records DEVERR_TIMEOUT in the context's error word and returns.
+__global__ void k_wait_selftest(int* err, long long limit)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0)
+        mbar_init(&bar, 1);
+    __syncwarp();
+    mbar_wait_limit(&bar, 0, threadIdx.x == 0 ? err : nullptr, limit);
+}
+
+extern "C" MHD_API int mhd_selftest_wait(mhd_ctx* c, double seconds)
+{
+    if (!c || !(seconds > 0.0) || seconds > 2.0)
+        return set_err(MHD_ERR_ARG);
+    int dev = 0, khz = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    const long long limit = (long long)(seconds * 1e3 * (double)(khz > 0 ? khz : 2000000));
+    k_wait_selftest<<<1, 32, 0, c->stream>>>(c->err_dev, limit);
+    CUDA_TRY(cudaGetLastError());
+    c->launch_count++;
+    return set_err(MHD_OK);
+}
+
 // -------------------------------------------------------------- profiling
 
 extern "C" MHD_API int mhd_profile(mhd_ctx* c, int enable)

@@ -47,20 +47,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 }
 
 // Waits for the phase with the given parity; returns false (and records
-// DEVERR_TIMEOUT) if it has not completed within kWaitLimitCycles.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err)
+// DEVERR_TIMEOUT) if it has not completed within `limit` SM cycles.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t parity, int* err, long long limit)
 {
     if (mbar_try_wait(bar, parity))
         return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kWaitLimitCycles) {
+        if (clock64() - t0 > limit) {
             if (err)
                 atomicOr(err, DEVERR_TIMEOUT);
             return false;
         }
     }
     return true;
+}
+
+// The same with the kernels' limit, kWaitLimitCycles.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err)
+{
+    return mbar_wait_limit(bar, parity, err, kWaitLimitCycles);
 }
 
 // Global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16.

@@ -140,6 +140,14 @@ MHD_API int mhd_get_time(mhd_ctx *ctx, double *t, double *dt, long long *steps);
 MHD_API int mhd_use_graphs(mhd_ctx *ctx, int enable);
 /* Synchronises and returns MHD_OK or the first device-side error recorded. */
 MHD_API int mhd_check(mhd_ctx *ctx);
+/* Clears the device-side error word (synchronous). */
+MHD_API int mhd_clear_errors(mhd_ctx *ctx);
+/* Self-test of the bounded device waits: queues a one-warp kernel that waits
+ * on a barrier nothing completes and gives up after `seconds` (0 < s <= 2),
+ * so that the next mhd_check returns MHD_ERR_TIMEOUT; the context stays
+ * usable (mhd_clear_errors, then step as usual).  No reference counterpart:
+ * the reference's CUDA path exits on any error (Cuda/cuda_function.h:4-12). */
+MHD_API int mhd_selftest_wait(mhd_ctx *ctx, double seconds);
 
 /* Per-kernel timing with CUDA events on the context stream (off by default;
  * while on, steps run as direct launches).  Kernel ids: */
