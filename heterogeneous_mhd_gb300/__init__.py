@@ -36,6 +36,8 @@ MHD_PLAIN, MHD_FUSED = 0, 1
 KERNELS = {"calcfl": 0, "fluidx": 1, "advectbyzx": 2, "transpose12": 3, "transpose13": 4,
            "copy": 5, "cfl_finalize": 6, "sweep": 7}
 
+DIAG_KEYS = ("min_rho", "min_p", "max_divb", "mass", "kinetic", "magnetic", "energy", "max_speed")
+
 _ERRORS = {1: "bad argument", 2: "CUDA runtime error", 3: "device-side wait timed out",
            4: "non-finite value in the CFL reduction", 5: "unsupported shape or mode",
            6: "device allocation failed"}
@@ -94,6 +96,7 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
                                    C.POINTER(C.c_longlong)]),
         "mhd_use_graphs": (C.c_int, [_vp, C.c_int]),
         "mhd_check": (C.c_int, [_vp]),
+        "mhd_diagnostics": (C.c_int, [_vp, C.POINTER(C.c_double)]),
         "mhd_clear_errors": (C.c_int, [_vp]),
         "mhd_selftest_wait": (C.c_int, [_vp, C.c_double]),
         "mhd_profile": (C.c_int, [_vp, C.c_int]),
@@ -304,6 +307,13 @@ class Context:
 
     def check(self) -> int:
         return lib().mhd_check(self._h)
+
+    def diagnostics(self) -> dict:
+        """Run diagnostics of the current state, reduced on the device in FP64:
+        min_rho, min_p, max_divb, mass, kinetic, magnetic, energy, max_speed."""
+        out = (C.c_double * len(DIAG_KEYS))()
+        _check(lib().mhd_diagnostics(self._h, out), "mhd_diagnostics")
+        return dict(zip(DIAG_KEYS, list(out)))
 
     def clear_errors(self) -> None:
         _check(lib().mhd_clear_errors(self._h), "mhd_clear_errors")

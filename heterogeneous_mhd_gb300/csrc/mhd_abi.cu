@@ -933,6 +933,118 @@ extern "C" MHD_API int mhd_divb_max(mhd_ctx* c, double* out)
     return set_err(MHD_OK);
 }
 
+// ----------------------------------------------------------- diagnostics
+
+// Per-block partials of the run diagnostics (MHD_DIAG_* order): min rho,
+// min p, max |div B|, sum rho, sum |m|^2/(2 rho), sum |B_c|^2/2, sum E,
+// max |v|, with B_c the cell-centred field (the mean of the two faces,
+// C/fluidx.c:71-81) and p = (gamma - 1)(E - |m|^2/(2 rho) - |B_c|^2/2).
+// FP64 accumulation; a NaN in rho or p propagates into the minima.
+template <typename R>
+__global__ void __launch_bounds__(256) k_diag(const R* __restrict__ u, const R* __restrict__ b, int nx, int ny,
+                                              int nz, double* part)
+{
+    constexpr int NQ = 8;
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    double acc[NQ] = {inf, inf, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const size_t ncell = (size_t)nx * ny * nz;
+    for (size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x; cell < ncell;
+         cell += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(cell % nx), j = (int)((cell / nx) % ny), k = (int)(cell / ((size_t)nx * ny));
+        const size_t ci = ((size_t)k * ny + j) * nx + ((i + 1 == nx) ? 0 : i + 1);
+        const size_t cj = ((size_t)k * ny + ((j + 1 == ny) ? 0 : j + 1)) * nx + i;
+        const size_t ck = ((size_t)((k + 1 == nz) ? 0 : k + 1) * ny + j) * nx + i;
+        const double rho = (double)u[cell * 5], mx = (double)u[cell * 5 + 1], my = (double)u[cell * 5 + 2];
+        const double mz = (double)u[cell * 5 + 3], e = (double)u[cell * 5 + 4];
+        const double b0 = (double)b[cell * 3], b1 = (double)b[cell * 3 + 1], b2 = (double)b[cell * 3 + 2];
+        const double bx = 0.5 * (b0 + (double)b[ci * 3]), by = 0.5 * (b1 + (double)b[cj * 3 + 1]);
+        const double bz = 0.5 * (b2 + (double)b[ck * 3 + 2]);
+        const double m2 = mx * mx + my * my + mz * mz;
+        const double ek = 0.5 * m2 / rho, em = 0.5 * (bx * bx + by * by + bz * bz);
+        const double p = (5.0 / 3.0 - 1.0) * (e - ek - em);
+        const double div = fabs(((double)b[ci * 3] - b0) + ((double)b[cj * 3 + 1] - b1) + ((double)b[ck * 3 + 2] - b2));
+        acc[0] = (rho < acc[0] || rho != rho) ? rho : acc[0];
+        acc[1] = (p < acc[1] || p != p) ? p : acc[1];
+        acc[2] = fmax(acc[2], div);
+        acc[3] += rho;
+        acc[4] += ek;
+        acc[5] += em;
+        acc[6] += e;
+        acc[7] = fmax(acc[7], sqrt(m2) / rho);
+    }
+    __shared__ double red[NQ][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        double x = acc[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_xor_sync(0xffffffffu, x, o);
+            if (q < 2)
+                x = (y < x || y != y) ? y : x;
+            else if (q == 2 || q == 7)
+                x = fmax(x, y);
+            else
+                x += y;
+        }
+        if (lane == 0)
+            red[q][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NQ) {
+        const int q = threadIdx.x;
+        double x = red[q][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            const double y = red[q][w];
+            if (q < 2)
+                x = (y < x || y != y) ? y : x;
+            else if (q == 2 || q == 7)
+                x = fmax(x, y);
+            else
+                x += y;
+        }
+        part[(size_t)blockIdx.x * NQ + q] = x;
+    }
+}
+
+extern "C" MHD_API int mhd_diagnostics(mhd_ctx* c, double* out)
+{
+    if (!c || !out || !c->have_state)
+        return set_err(MHD_ERR_ARG);
+    constexpr int NQ = MHD_DIAG_COUNT;
+    const size_t cells = ncell(c);
+    int blocks = (int)((cells + 255) / 256);
+    if (blocks > 1024)
+        blocks = 1024;
+    MHD_TRY(set_err(c->divb.ensure((size_t)blocks * NQ * sizeof(double))));
+    double* part = static_cast<double*>(c->divb.p);
+    if (c->elem == 4)
+        k_diag<float><<<blocks, 256, 0, c->stream>>>(static_cast<const float*>(c->U[0].p),
+                                                     static_cast<const float*>(c->B[0].p), c->nx, c->ny, c->nz, part);
+    else
+        k_diag<double><<<blocks, 256, 0, c->stream>>>(static_cast<const double*>(c->U[0].p),
+                                                      static_cast<const double*>(c->B[0].p), c->nx, c->ny, c->nz, part);
+    CUDA_TRY(cudaGetLastError());
+    c->launch_count++;
+    std::vector<double> h((size_t)blocks * NQ);
+    if (cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    for (int q = 0; q < NQ; q++) {
+        double x = h[q];
+        for (int blk = 1; blk < blocks; blk++) {
+            const double y = h[(size_t)blk * NQ + q];
+            if (q < 2)
+                x = (y < x || y != y) ? y : x;
+            else if (q == MHD_DIAG_MAX_DIVB || q == MHD_DIAG_MAX_SPEED)
+                x = y > x ? y : x;
+            else
+                x += y;
+        }
+        out[q] = x;
+    }
+    return set_err(MHD_OK);
+}
+
 // ----------------------------------------------------------- drop-in layer
 
 static std::mutex g_dropin_mu;

@@ -180,6 +180,23 @@ MHD_API long long mhd_launch_count(mhd_ctx *ctx);
 MHD_API int mhd_tune_set(const char *key, int value);
 MHD_API int mhd_tune_get(const char *key);
 
+/* Run diagnostics of the current state, reduced on the device in FP64
+ * (synchronous): out[MHD_DIAG_COUNT] in the order below.  B_c is the
+ * cell-centred field (mean of the two faces of the cell), p = (5/3 - 1) *
+ * (E - |m|^2/(2 rho) - |B_c|^2/2).  A NaN density or pressure propagates into
+ * the minima.  No reference counterpart (the reference prints two sample
+ * values per step, C/mhd.c:66). */
+#define MHD_DIAG_MIN_RHO 0
+#define MHD_DIAG_MIN_P 1
+#define MHD_DIAG_MAX_DIVB 2
+#define MHD_DIAG_MASS 3
+#define MHD_DIAG_KINETIC 4
+#define MHD_DIAG_MAGNETIC 5
+#define MHD_DIAG_ENERGY 6
+#define MHD_DIAG_MAX_SPEED 7
+#define MHD_DIAG_COUNT 8
+MHD_API int mhd_diagnostics(mhd_ctx *ctx, double *out);
+
 /* max |div B| of the current state, computed on the device (synchronous). */
 MHD_API int mhd_divb_max(mhd_ctx *ctx, double *out);
 

@@ -68,3 +68,58 @@ def test_checkpoint_resume_is_bitwise(exact, mhd, cuda, tmp_path):
         assert ctx.check() == mhd.MHD_OK
     assert bitwise_equal(ur, uf) and bitwise_equal(br, bf)
     assert np.float32(tr) == np.float32(tf) and np.float32(dtr) == np.float32(dtf)
+
+
+def numpy_diagnostics(u, b, shape):
+    nx, ny, nz = shape
+    U = u.reshape(nz, ny, nx, 5).astype(np.float64)
+    B = b.reshape(nz, ny, nx, 3).astype(np.float64)
+    rho, m, e = U[..., 0], U[..., 1:4], U[..., 4]
+    bx = 0.5 * (B[..., 0] + np.roll(B[..., 0], -1, axis=2))
+    by = 0.5 * (B[..., 1] + np.roll(B[..., 1], -1, axis=1))
+    bz = 0.5 * (B[..., 2] + np.roll(B[..., 2], -1, axis=0))
+    m2 = (m ** 2).sum(-1)
+    ek, em = 0.5 * m2 / rho, 0.5 * (bx ** 2 + by ** 2 + bz ** 2)
+    p = (5.0 / 3.0 - 1.0) * (e - ek - em)
+    div = np.abs((np.roll(B[..., 0], -1, axis=2) - B[..., 0]) + (np.roll(B[..., 1], -1, axis=1) - B[..., 1])
+                 + (np.roll(B[..., 2], -1, axis=0) - B[..., 2]))
+    return {"min_rho": rho.min(), "min_p": p.min(), "max_divb": div.max(), "mass": rho.sum(), "kinetic": ek.sum(),
+            "magnetic": em.sum(), "energy": e.sum(), "max_speed": (np.sqrt(m2) / rho).max()}
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+def test_diagnostics_match_numpy(fp64, mhd, cuda):
+    shape = (24, 16, 16)
+    u, b = mhd.init_vortex(*shape, seed=5)
+    if fp64:
+        u, b = u.astype(np.float64), b.astype(np.float64)
+    with mhd.Context(*shape, fp64=fp64) as ctx:
+        ctx.set_state(u, b)
+        ctx.step(2)
+        su, sb = ctx.get_state()
+        d = ctx.diagnostics()
+    ref = numpy_diagnostics(su, sb, shape)
+    for key, val in ref.items():
+        assert d[key] == pytest.approx(val, rel=1e-12, abs=1e-14), key
+
+
+def test_run_driver_log_checkpoint_and_resume(mhd, cuda, tmp_path):
+    from heterogeneous_mhd_gb300 import run
+    log, chk = tmp_path / "run.jsonl", tmp_path / "run.chk"
+    cfg = run.parse(["--n", "32", "--ic", "turbulence", "--seed", "2", "--steps", "6", "--every", "2",
+                     "--log", str(log), "--checkpoint", str(chk), "--checkpoint-every", "4"])
+    recs = run.run(cfg)
+    lines = [__import__("json").loads(x) for x in log.read_text().splitlines()]
+    assert [r["step"] for r in lines] == [0, 2, 4, 6] and lines == recs
+    assert all(r["status"] == 0 for r in lines)
+    m0 = lines[0]["mass"]
+    assert all(abs(r["mass"] - m0) <= 1e-5 * m0 for r in lines)
+    assert all(r["max_divb"] < 1e-4 for r in lines) and all(r["min_p"] > 0 for r in lines)
+    # the final checkpoint (step 6) resumed for 2 steps equals 8 uninterrupted steps
+    more = run.run(run.parse(["--resume", str(chk), "--steps", "2", "--every", "2",
+                              "--log", str(tmp_path / "more.jsonl")]))
+    straight = run.run(run.parse(["--n", "32", "--ic", "turbulence", "--seed", "2", "--steps", "8", "--every", "8",
+                                  "--log", str(tmp_path / "straight.jsonl")]))
+    assert more[-1]["step"] == straight[-1]["step"] == 8
+    for key in ("t", "dt", "min_rho", "min_p", "max_divb", "mass", "kinetic", "magnetic", "energy", "max_speed"):
+        assert more[-1][key] == straight[-1][key], key
