@@ -150,9 +150,22 @@ def cpu_baseline(size: int, seconds: float = 12.0):
         if time.perf_counter() - t0 > seconds:
             break
     el = time.perf_counter() - t0
+    # one core, as the reference's C path runs when built as shipped (64^3, a few seconds)
+    port.set_threads(1)
+    u1, b1 = mhd.init_vortex(64, 64, 64, seed=0)
+    t1, steps1 = time.perf_counter(), 0
+    while True:
+        u1, b1, _, _, _ = port.strang(u1, b1, 64, 64, 64, 1)
+        steps1 += 1
+        if time.perf_counter() - t1 > 3.0:
+            break
+    single = 64 ** 3 * steps1 / (time.perf_counter() - t1)
+    port.set_threads(cores)
     return {"value": size ** 3 * steps / el, "unit": "cell-updates/s", "cores": cores, "kind": "port",
             "sample": f"{steps} full Strang steps of the {size}^3 turbulence box, oracle restatement of the "
-                      f"reference C path with OpenMP over pencils ({cores} threads)"}
+                      f"reference C path with OpenMP over pencils ({cores} threads)",
+            "single_core": {"value": single, "unit": "cell-updates/s", "cores": 1,
+                            "sample": f"{steps1} Strang steps of the 64^3 vortex on one thread"}}
 
 
 def reference_arm(args):
