@@ -222,7 +222,7 @@ struct A3Plan {
     int C, T, NS, J, K;
 };
 
-static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax = 0)
+static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax = 0, int uc = 5)
 {
     if (!kV2 || !aligned)
         return false;
@@ -233,15 +233,15 @@ static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax
     p.T = nx / p.C;
     if (!(p.C == 4 ? pow2_in(p.T, 8, 128) : pow2_in(p.T, 4, 64)))
         return false;
-    const int ctas = (p.NS == 2) ? 3 : 2;
+    const int ctas = ((p.NS == 2) ? 3 : 2) + (uc < 5 ? 1 : 0);  // the side array leaves room for one more
     const size_t smem_cap = (size_t)(224 * 1024) / ctas;
     const int jt = tune_value(TUNE_ADVECT_J);
     p.J = 0;
     for (int j = 1; j <= ny && j <= 16; j++) {
-        const bool fits = advect3_threads(j, p.T) <= 384 && advect3_smem_floats(j, nx, p.NS, ax) * sizeof(float) <= 227 * 1024;
+        const bool fits = advect3_threads(j, p.T) <= 384 && advect3_smem_floats(j, nx, p.NS, ax, uc) * sizeof(float) <= 227 * 1024;
         if (ny % j != 0 || !fits)
             continue;
-        if (jt ? (j == jt) : (advect3_smem_floats(j, nx, p.NS, ax) * sizeof(float) <= smem_cap))
+        if (jt ? (j == jt) : (advect3_smem_floats(j, nx, p.NS, ax, uc) * sizeof(float) <= smem_cap))
             p.J = j;
     }
     if (!p.J)
@@ -257,30 +257,30 @@ static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax
     return true;
 }
 
-template <int C, int T, int NS, int AX = 0>
+template <int C, int T, int NS, int AX = 0, bool WU = false>
 static cudaError_t launch_ad3(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    cudaError_t e = allow_smem(k_advect3<EX, C, T, NS, AX>, attr, AX == 0);
+    cudaError_t e = allow_smem(k_advect3<EX, C, T, NS, AX, WU>, attr, AX == 0);
     if (e != cudaSuccess)
         return e;
     const int nj = (AX == 0) ? a.ny : a.nx, nk = (AX == 2) ? a.ny : a.nz;
     dim3 grid(nj / a.P, nk / a.K, a.bs.count);
-    k_advect3<EX, C, T, NS, AX><<<grid, advect3_threads(a.P, T), advect3_smem_floats(a.P, C * T, NS, AX) * sizeof(float),
-                                  s>>>(a);
+    k_advect3<EX, C, T, NS, AX, WU><<<grid, advect3_threads(a.P, T),
+                                      advect3_smem_floats(a.P, C * T, NS, AX, WU ? 2 : 5) * sizeof(float), s>>>(a);
     return cudaGetLastError();
 }
 
-template <int C, int NS, int AX = 0>
+template <int C, int NS, int AX = 0, bool WU = false>
 static cudaError_t launch_ad3_t(const AdvectArgs& a, int T, cudaStream_t s)
 {
     switch (T) {
-    case 4: if constexpr (C == 8) return launch_ad3<C, 4, NS, AX>(a, s); break;
-    case 8: return launch_ad3<C, 8, NS, AX>(a, s);
-    case 16: return launch_ad3<C, 16, NS, AX>(a, s);
-    case 32: return launch_ad3<C, 32, NS, AX>(a, s);
-    case 64: return launch_ad3<C, 64, NS, AX>(a, s);
-    case 128: if constexpr (C == 4) return launch_ad3<C, 128, NS, AX>(a, s); break;
+    case 4: if constexpr (C == 8) return launch_ad3<C, 4, NS, AX, WU>(a, s); break;
+    case 8: return launch_ad3<C, 8, NS, AX, WU>(a, s);
+    case 16: return launch_ad3<C, 16, NS, AX, WU>(a, s);
+    case 32: return launch_ad3<C, 32, NS, AX, WU>(a, s);
+    case 64: return launch_ad3<C, 64, NS, AX, WU>(a, s);
+    case 128: if constexpr (C == 4) return launch_ad3<C, 128, NS, AX, WU>(a, s); break;
     }
     return cudaErrorInvalidValue;
 }
@@ -397,7 +397,14 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
         A4Plan p4;
         if (plan_advect4(a, (al & 15) == 0, p4))
             return advect_x4(a, p4, s);
+        // the (rho, m_x) side array of the fluidx before, when given, replaces u in the slabs
+        const bool wu = a.w != nullptr && (reinterpret_cast<uintptr_t>(a.w) & 15) == 0 && a.bs.count == 1;
         A3Plan p3;
+        if (wu && plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3, 0, 2) && p3.C == 4) {
+            a.P = p3.J;
+            a.K = p3.K;
+            return (p3.NS == 2) ? launch_ad3_t<4, 2, 0, true>(a, p3.T, s) : launch_ad3_t<4, 3, 0, true>(a, p3.T, s);
+        }
         if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3)) {
             a.P = p3.J;
             a.K = p3.K;
@@ -508,8 +515,16 @@ static int fused_ok(int nx, int ny, int nz)
            plan_advect3(nz, nx, ny, true, q, 2);
 }
 
+// nonzero if the x-sweep fluidx of this grid is k_fluidx2 (which writes the
+// (rho, m_x) side array when asked)
+static int fluidx_writes_w(int nx, int ny, int nz, int aligned)
+{
+    (void)nz;
+    return kV2 && plan_fluidx(nx, ny, aligned != 0).C != 0;
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
-                               sizeof(CflPart<R>), fluidx_parts, fused_ok};
+                               sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

@@ -40,15 +40,20 @@ __host__ __device__ inline int advect3_threads(int J, int T)
 // shared memory in floats: NS u slabs, NS b slabs, FA[J+1][n], FB[2][J][n],
 // B3[2][J][n], seam, and for the y/z sweeps the output rows [J][n][3]; plus
 // the mbarriers (in the static part)
-__host__ __device__ inline size_t advect3_smem_floats(int J, int n, int NS, int ax = 0)
+// (uc: floats per cell of a staged u pencil: 5, or 2 for the (rho, m_x) side
+// array of the fluidx before)
+__host__ __device__ inline size_t advect3_smem_floats(int J, int n, int NS, int ax = 0, int uc = 5)
 {
     const size_t pad = ax ? kSweepPad : 0;
-    const size_t uslab = (size_t)(J + 2) * (n * 5 + pad), bslab = (size_t)(J + 1) * (n * 3 + pad);
+    const size_t uslab = (size_t)(J + 2) * (n * uc + pad), bslab = (size_t)(J + 1) * (n * 3 + pad);
     return NS * uslab + NS * bslab + (size_t)(J + 1) * n + (size_t)4 * J * n + 2 * 32 * kSeamVals +
            (ax ? (size_t)J * (3 * n + pad) : 0);
 }
 
-template <bool EX, int C, int T, int NS, int AX = 0>
+// WU (x sweep only): the u slabs hold the (rho, m_x) side array a.w written
+// by the fluidx before (8 instead of 20 bytes per cell of HBM traffic and of
+// shared memory).
+template <bool EX, int C, int T, int NS, int AX = 0, bool WU = false>
 __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
 {
     select_box(a, blockIdx.z);
@@ -69,7 +74,9 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     const int j0 = blockIdx.x * J, k0 = blockIdx.y * K;
     const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
 
-    constexpr int UROW = n * 5 + (AX ? kSweepPad : 0), BROW = n * 3 + (AX ? kSweepPad : 0);  // pencil strides
+    static_assert(!WU || AX == 0, "the side array is written by the x-sweep fluidx");
+    constexpr int UC = WU ? 2 : 5;  // floats per cell of a staged u pencil
+    constexpr int UROW = n * UC + (AX ? kSweepPad : 0), BROW = n * 3 + (AX ? kSweepPad : 0);  // pencil strides
     const size_t uslab = (size_t)(J + 2) * UROW, bslab = (size_t)(J + 1) * BROW;
     float* U = reinterpret_cast<float*>(smem_raw);  // [NS][J+2][n*5]
     float* B = U + NS * uslab;                        // [NS][J+1][n*3]
@@ -81,6 +88,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
 
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
+    const float* usrc = WU ? static_cast<const float*>(a.w) : uu;  // what the u slabs hold
 
     // ---- slab loads: plane p into ring slot s (one mbarrier per slot),
     // issued by warp 0: lane 0 registers the bytes, one lane per pencil copies.
@@ -89,13 +97,13 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         if constexpr (AX == 0) {
             if (tid < 32) {
                 if (tid == 0)
-                    mbar_arrive_expect_tx(&bar[s], (uint32_t)((J + 2) * n * 20 + (J + 1) * n * 12));
+                    mbar_arrive_expect_tx(&bar[s], (uint32_t)((J + 2) * n * UC * 4 + (J + 1) * n * 12));
                 __syncwarp();
                 for (int row = tid; row < J + 2; row += 32) {
                     int j = j0 - 1 + row;
                     j = (j < 0) ? j + ny : (j >= ny ? j - ny : j);
                     const size_t cell = ((size_t)pp * ny + j) * n;
-                    tma_load_1d(U + s * uslab + (size_t)row * UROW, uu + cell * 5, n * 20, &bar[s]);
+                    tma_load_1d(U + s * uslab + (size_t)row * UROW, usrc + cell * UC, n * UC * 4, &bar[s]);
                 }
                 for (int row = tid; row < J + 1; row += 32) {
                     int j = j0 + row;
@@ -133,18 +141,21 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     auto parity_of = [&](int p) { return (uint32_t)(((p - k0 + 1) / NS) & 1); };
 
     // this thread's chunk of u pencil `row` (0 = j0-1) / b pencil `row` (0 = j0) in slot s
-    auto u_chunk = [&](int s, int row, float (&out)[C * 5]) {
-        lds_chunk<float, C * 5>(U + s * uslab + (size_t)row * UROW + g.t * C * 5, out);
+    auto u_chunk = [&](int s, int row, float (&out)[C * UC]) {
+        lds_chunk<float, C * UC>(U + s * uslab + (size_t)row * UROW + g.t * C * UC, out);
     };
     auto b_chunk = [&](int s, int row, float (&out)[C * 3]) {
         lds_chunk<float, C * 3>(B + s * bslab + (size_t)row * BROW + g.t * C * 3, out);
     };
     // raw face velocity between two u chunks (C/advectbyzxA1.c:34, C/advectbyzxB1.c:34)
     constexpr int UM = sweep_u<AX>(1), BD = sweep_b<AX>(0), BJ = sweep_b<AX>(1), BK = sweep_b<AX>(2);
-    auto face_v = [&](const float (&um)[C * 5], const float (&uc)[C * 5], float (&vr)[C]) {
+    auto face_v = [&](const float (&um)[C * UC], const float (&uc)[C * UC], float (&vr)[C]) {
 #pragma unroll
         for (int m = 0; m < C; m++) {
-            vr[m] = tvdb_face<float, EX>(um[5 * m + UM], uc[5 * m + UM], um[5 * m], uc[5 * m]);
+            if constexpr (WU)
+                vr[m] = tvdb_face<float, EX>(um[2 * m + 1], uc[2 * m + 1], um[2 * m], uc[2 * m]);
+            else
+                vr[m] = tvdb_face<float, EX>(um[5 * m + UM], uc[5 * m + UM], um[5 * m], uc[5 * m]);
         }
     };
 
@@ -164,7 +175,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
     const int bp = r - J - 1;
     {
         const int sm = slot_of(k0 - 1), sc = slot_of(k0);
-        float um[C * 5], uc[C * 5], bb[C * 3], vr[C], bv[C], F[C], bn[C];
+        float um[C * UC], uc[C * UC], bb[C * 3], vr[C], bv[C], F[C], bn[C];
         const int prow = brow ? bp + 1 : 1;  // u row of pencil j0+bp
         u_chunk(sm, prow, um);
         u_chunk(sc, prow, uc);
@@ -198,7 +209,7 @@ __global__ void __launch_bounds__(384) k_advect3(AdvectArgs a)
         // ---- rows: A at plane k (r <= J), B at plane k+1 (r > J)
         float F[C], bn[C], b1own[C];
         {
-            float um[C * 5], uc[C * 5], bb[C * 3], vr[C], bv[C];
+            float um[C * UC], uc[C * UC], bb[C * 3], vr[C], bv[C];
             if (r <= J) {
                 u_chunk(sk, r, um);      // pencil j0+r-1
                 u_chunk(sk, r + 1, uc);  // pencil j0+r

@@ -304,6 +304,18 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
             }
         // own cells: no other thread reads them after the gather
         sts_chunk<R, C * 5>(su + (size_t)lp * SU + (size_t)i0 * 5, of);
+        // the two values the next advectbyzx reads (rho, m_x), 8 bytes per cell
+        if constexpr (AX == 0 && sizeof(R) == 4) {
+            if (a.w_out) {
+                float wv[2 * C];
+#pragma unroll
+                for (int m = 0; m < C; m++) {
+                    wv[2 * m] = q[m][0];
+                    wv[2 * m + 1] = q[m][1];
+                }
+                stg_chunk<float, 2 * C>(static_cast<float*>(a.w_out) + 2 * (c0 + (size_t)lp * n + i0), wv);
+            }
+        }
     }
 
     // ---- optional calcfl epilogue on the new state (face b at (j,k)); x sweep only

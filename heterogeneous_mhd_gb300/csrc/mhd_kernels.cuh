@@ -45,6 +45,7 @@ struct FluidxArgs {
     int* err;
     BoxStrides bs;
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
+    void* w_out;          // optional (FP32, x sweep, one box): (rho, m_x) of the new state, 2 values per cell
 };
 
 struct AdvectArgs {
@@ -60,6 +61,7 @@ struct AdvectArgs {
     int K;                // planes per CTA along k for the marching kernel (nz % K == 0)
     BoxStrides bs;
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
+    const void* w;        // optional (FP32, x sweep, one box): (rho, m_x) of update_u, 2 values per cell
 };
 
 struct TransposeArgs {

@@ -25,6 +25,8 @@ struct KernelSet {
     int (*fluidx_parts)(int nx, int ny, int nz, int aligned);
     // nonzero if the sweeps along y and z of the fused step have kernels for this grid
     int (*fused_ok)(int nx, int ny, int nz);
+    // nonzero if the x-sweep fluidx of this grid writes the (rho, m_x) side array (FluidxArgs::w_out)
+    int (*fluidx_writes_w)(int nx, int ny, int nz, int aligned);
 };
 
 const KernelSet* kernels_f32_fast();

@@ -116,6 +116,57 @@ __device__ __forceinline__ void scatter_tile(float* dst_row0, size_t rstride, co
 // element by element: keeps the shared stores of a warp within 2-way conflicts
 constexpr int kSweepPad = 8;
 
+// Global chunk loads/stores of NF consecutive values with the widest vector
+// the alignment allows (the caller guarantees it: 16 B for NF % 4 == 0, 8 B
+// for NF % 2 == 0).
+template <typename R, int NF>
+__device__ __forceinline__ void ldg_chunk(const R* src, R (&dst)[NF])
+{
+    if constexpr (sizeof(R) == 4 && NF % 4 == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+        for (int v = 0; v < NF / 4; v++) {
+            const float4 x = __ldg(s4 + v);
+            dst[4 * v] = x.x;
+            dst[4 * v + 1] = x.y;
+            dst[4 * v + 2] = x.z;
+            dst[4 * v + 3] = x.w;
+        }
+    } else if constexpr (sizeof(R) == 4 && NF % 2 == 0) {
+        const float2* s2 = reinterpret_cast<const float2*>(src);
+#pragma unroll
+        for (int v = 0; v < NF / 2; v++) {
+            const float2 x = __ldg(s2 + v);
+            dst[2 * v] = x.x;
+            dst[2 * v + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NF; v++)
+            dst[v] = src[v];
+    }
+}
+
+template <typename R, int NF>
+__device__ __forceinline__ void stg_chunk(R* dst, const R (&src)[NF])
+{
+    if constexpr (sizeof(R) == 4 && NF % 4 == 0) {
+        float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+        for (int v = 0; v < NF / 4; v++)
+            d4[v] = make_float4(src[4 * v], src[4 * v + 1], src[4 * v + 2], src[4 * v + 3]);
+    } else if constexpr (sizeof(R) == 4 && NF % 2 == 0) {
+        float2* d2 = reinterpret_cast<float2*>(dst);
+#pragma unroll
+        for (int v = 0; v < NF / 2; v++)
+            d2[v] = make_float2(src[2 * v], src[2 * v + 1]);
+    } else {
+#pragma unroll
+        for (int v = 0; v < NF; v++)
+            dst[v] = src[v];
+    }
+}
+
 template <typename R, int NF>
 __device__ __forceinline__ void lds_chunk(const R* src, R (&dst)[NF])
 {
