@@ -523,8 +523,16 @@ static int fluidx_writes_w(int nx, int ny, int nz, int aligned)
     return kV2 && plan_fluidx(nx, ny, aligned != 0).C != 0;
 }
 
+// nonzero if the transpose of this grid is k_transpose3 (which writes the side
+// array when asked); nx, ny, nz are the input dims, the buffers 16-byte aligned
+static int transpose_writes_w(int axis, int nx, int ny, int nz)
+{
+    const int na = (axis == 1) ? ny : nz;
+    return kV2 && nx % kT3 == 0 && na % kT3 == 0;
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
-                               sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w};
+                               sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w, transpose_writes_w};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

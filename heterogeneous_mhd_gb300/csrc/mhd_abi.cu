@@ -358,13 +358,14 @@ static int op_advect(mhd_ctx* c, void* b_out, const void* b1_src, const void* uu
 }
 
 static int op_transpose(mhd_ctx* c, int axis, void* u, void* b, const void* uu, const void* ub, int nx, int ny,
-                        int nz)
+                        int nz, void* w_out = nullptr)
 {
     if (nx <= 0 || ny <= 0 || nz <= 0)
         return MHD_ERR_ARG;
     if (axis == 2 && nx != nz)
         return MHD_ERR_ARG;
     TransposeArgs a{u, b, uu, ub, nx, ny, nz, axis};
+    a.w_out = w_out;
     KTimer kt(c, axis == 1 ? MHD_K_TRANSPOSE12 : MHD_K_TRANSPOSE13);
     CUDA_TRY(c->ks->transpose(a, c->stream));
     return MHD_OK;
@@ -654,13 +655,18 @@ static int enqueue_plain_step(mhd_ctx* c, double cfl)
     MHD_TRY(op_advect(c, B1, B0, U1, B0, nz, nx, ny, 0, dt, 0, W));
     MHD_TRY(op_advect(c, B0, B1, U1, B1, nz, nx, ny, 0, dt, 0, W));
     MHD_TRY(op_fluidx(c, U0, U1, B0, nz, nx, ny, 0, dt, nullptr));
-    // back
-    MHD_TRY(op_transpose(c, 2, U1, B1, U0, B0, nz, nx, ny));
-    MHD_TRY(op_advect(c, B0, B1, U1, B1, ny, nx, nz, 0, dt));
+    // back (the transposes write the side array of their output for the advectbyzx after them)
+    auto tside = [&](int axis, int ax, int ay, int az) -> void* {
+        return (c->W.p && c->ks->transpose_writes_w(axis, ax, ay, az)) ? c->W.p : nullptr;
+    };
+    W = tside(2, nz, nx, ny);
+    MHD_TRY(op_transpose(c, 2, U1, B1, U0, B0, nz, nx, ny, W));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, ny, nx, nz, 0, dt, 0, W));
     MHD_TRY(op_fluidx(c, U0, U1, B0, ny, nx, nz, 0, dt, nullptr));
     // x again
-    MHD_TRY(op_transpose(c, 1, U1, B1, U0, B0, ny, nx, nz));
-    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt));
+    W = tside(1, ny, nx, nz);
+    MHD_TRY(op_transpose(c, 1, U1, B1, U0, B0, ny, nx, nz, W));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0, W));
     // last fluidx with the calcfl epilogue for the next step
     const size_t nparts = fluidx_parts(c);
     if (c->part.cap < nparts * c->ks->part_bytes)  // sized by mhd_set_state

@@ -72,6 +72,7 @@ struct TransposeArgs {
     int nx, ny, nz;
     int axis;             // 1: x<->y (transpose12), 2: x<->z (transpose13, nx == nz)
     BoxStrides bs;
+    void* w_out;          // optional (FP32 tiled kernel, one box): (rho, m_x) of the output, 2 values per cell
 };
 
 // Offset every array of a launch to box `box` (the per-CTA partials of the

@@ -27,6 +27,8 @@ struct KernelSet {
     int (*fused_ok)(int nx, int ny, int nz);
     // nonzero if the x-sweep fluidx of this grid writes the (rho, m_x) side array (FluidxArgs::w_out)
     int (*fluidx_writes_w)(int nx, int ny, int nz, int aligned);
+    // nonzero if the transpose (axis 1 or 2) of this grid writes it (TransposeArgs::w_out)
+    int (*transpose_writes_w)(int axis, int nx, int ny, int nz);
 };
 
 const KernelSet* kernels_f32_fast();

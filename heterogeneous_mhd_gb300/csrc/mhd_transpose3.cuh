@@ -6,7 +6,9 @@
 // so a whole tile per CTA is in flight instead of what registers can hold.
 // Each warp then writes whole output rows: lane l writes floats l, l+32, ...
 // of a row, whose (cell, component) source offsets are fixed per lane and
-// computed once.
+// computed once.  With w_out it also writes the first two components of the
+// output cells (rho and the new m_x) as the side array the next advectbyzx
+// reads.
 #pragma once
 #include "mhd_kernels.cuh"
 
@@ -46,11 +48,16 @@ __global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
     }
     // per-lane source offsets inside a transposed row: output float f = l + 32q
     // is component c of output cell aa = f / 5, read from tile row aa
-    int su_off[5], sb_off[3];
+    int su_off[5], sb_off[3], sw_off[2];
 #pragma unroll
     for (int q = 0; q < 5; q++) {
         const int f = lane + 32 * q, aa = f / 5, c = f - 5 * aa;
         su_off[q] = aa * kT3U + perm_u<AXIS>(c);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {  // side array: components 0, 1 of the output cells
+        const int f = lane + 32 * q, aa = f / 2, c = f - 2 * aa;
+        sw_off[q] = aa * kT3U + perm_u<AXIS>(c);
     }
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -61,6 +68,7 @@ __global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
 
     float* uo = static_cast<float*>(a.u_out);
     float* bo = static_cast<float*>(a.b_out);
+    float* wo = static_cast<float*>(a.w_out);
 #pragma unroll
     for (int s = 0; s < kT3 / 8; s++) {
         const int i = warp + 8 * s;  // output row: position i0+i of the other axis
@@ -73,6 +81,11 @@ __global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
 #pragma unroll
         for (int q = 0; q < 3; q++)
             brow[lane + 32 * q] = sb[sb_off[q] + 3 * i];
+        if (wo) {
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+                wo[cout * 2 + lane + 32 * q] = su[sw_off[q] + 5 * i];
+        }
     }
 }
 
