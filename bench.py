@@ -39,11 +39,22 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# algorithmic HBM bytes per cell for one launch of each kernel (FP32 AoS:
-# u 20 B, b 12 B per cell)
-ALG_BYTES = {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 64, "calcfl": 32, "copy": 64,
-             "cfl_finalize": 0, "sweep": 64}
+# algorithmic HBM bytes per cell of one launch of each kernel, averaged over
+# the launches of a step (FP32 AoS: u 20 B, b 12 B per cell).  Plain step:
+# the three forward fluidx launches and the two backward transposes also write
+# the (rho, m_x) side array (8 B), and every advectbyzx reads it in place of u
+# (8 B instead of 20).  Fused step: no side array.
+ALG_BYTES = {
+    "plain": {"fluidx": 52 + 8 * 3 / 6, "advectbyzx": 32, "transpose12": 64 + 8 / 2, "transpose13": 64 + 8 / 2,
+              "calcfl": 32, "copy": 64, "cfl_finalize": 0, "sweep": 64},
+    "fused": {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 64, "calcfl": 32, "copy": 64,
+              "cfl_finalize": 0, "sweep": 64},
+}
+# per-cell bytes of a whole step in the survey's fixed convention (the
+# reference's operator sequence: 6 fluidx x 52 + 6 advectbyzx x 44 + 4
+# transposes x 64 + a calcfl 32), and what this step moves
 STEP_BYTES = {"plain": 864, "fused": 320}
+STEP_MOVED = {"plain": 6 * 52 + 3 * 8 + 6 * 32 + 4 * 64 + 2 * 8, "fused": 6 * 52 + 6 * 44}
 METRIC = "cell-updates/s at 256^3 (plain vs fused); closure speedup at matched error"
 
 
@@ -369,8 +380,10 @@ def our_arm(args):
     traffic = measured_traffic(dom, n)
     tot_ms, nl = kern[dom]
     mean_ms = tot_ms / nl
-    achieved = ALG_BYTES[dom] * cells / (mean_ms * 1e-3) / 1e9
+    alg = ALG_BYTES[args.variant][dom]
+    achieved = alg * cells / (mean_ms * 1e-3) / 1e9
     step_bw = STEP_BYTES[args.variant] * cells / (ms / args.steps * 1e-3) / 1e9
+    moved_bw = STEP_MOVED[args.variant] * cells / (ms / args.steps * 1e-3) / 1e9
     if rank != 0:
         ctx.close()
         rep.close()
@@ -387,8 +400,10 @@ def our_arm(args):
                 "d2h_bytes_per_step": 32 * cells, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
-                     "alg_bytes_per_launch": ALG_BYTES[dom] * cells, "mean_launch_ms": mean_ms,
-                     "step_alg_gbs": step_bw, "step_frac": step_bw / hbm},
+                     "alg_bytes_per_launch": alg * cells, "mean_launch_ms": mean_ms,
+                     "step_alg_gbs": step_bw, "step_frac": step_bw / hbm,
+                     "step_moved_bytes_per_cell": STEP_MOVED[args.variant], "step_moved_gbs": moved_bw,
+                     "step_moved_frac": moved_bw / hbm},
         "kernels": {k: {"ms_total": round(v[0], 4), "launches": v[1], "share": share.get(k, 0.0)}
                     for k, v in kern.items() if v[1] > 0},
         "profiled_ms_per_step": ms_profiled / args.steps,
