@@ -398,7 +398,8 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
         if (plan_advect4(a, (al & 15) == 0, p4))
             return advect_x4(a, p4, s);
         // the (rho, m_x) side array of the fluidx before, when given, replaces u in the slabs
-        const bool wu = a.w != nullptr && (reinterpret_cast<uintptr_t>(a.w) & 15) == 0 && a.bs.count == 1;
+        const bool wu = a.w != nullptr && (reinterpret_cast<uintptr_t>(a.w) & 15) == 0 &&
+                        (a.bs.count == 1 || a.bs.w % 16 == 0);
         A3Plan p3;
         if (wu && plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3, 0, 2) && p3.C == 4) {
             a.P = p3.J;

@@ -22,6 +22,7 @@ struct BoxStrides {
     size_t u = 0;   // bytes between the u arrays of consecutive boxes
     size_t b = 0;   // bytes between the b arrays
     size_t dt = 0;  // bytes between the device clocks (dt) of consecutive boxes
+    size_t w = 0;   // bytes between the (rho, m_x) side arrays
     int count = 1;  // boxes in the launch (the launchers' grid z extent)
 };
 
@@ -45,7 +46,7 @@ struct FluidxArgs {
     int* err;
     BoxStrides bs;
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
-    void* w_out;          // optional (FP32, x sweep, one box): (rho, m_x) of the new state, 2 values per cell
+    void* w_out;          // optional (FP32, x sweep): (rho, m_x) of the new state, 2 values per cell
 };
 
 struct AdvectArgs {
@@ -61,7 +62,7 @@ struct AdvectArgs {
     int K;                // planes per CTA along k for the marching kernel (nz % K == 0)
     BoxStrides bs;
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
-    const void* w;        // optional (FP32, x sweep, one box): (rho, m_x) of update_u, 2 values per cell
+    const void* w;        // optional (FP32, x sweep): (rho, m_x) of update_u, 2 values per cell
 };
 
 struct TransposeArgs {
@@ -72,7 +73,7 @@ struct TransposeArgs {
     int nx, ny, nz;
     int axis;             // 1: x<->y (transpose12), 2: x<->z (transpose13, nx == nz)
     BoxStrides bs;
-    void* w_out;          // optional (FP32 tiled kernel, one box): (rho, m_x) of the output, 2 values per cell
+    void* w_out;          // optional (FP32 tiled kernel): (rho, m_x) of the output, 2 values per cell
 };
 
 // Offset every array of a launch to box `box` (the per-CTA partials of the
@@ -84,6 +85,7 @@ __device__ __forceinline__ void select_box(FluidxArgs& a, int box, size_t part_b
     a.ub = box_ptr(a.ub, a.bs.b, box);
     a.dt_ptr = box_ptr(a.dt_ptr, a.bs.dt, box);
     a.cfl_part = box_ptr(a.cfl_part, part_bytes * gridDim.x * gridDim.y, box);
+    a.w_out = box_ptr(a.w_out, a.bs.w, box);
 }
 
 __device__ __forceinline__ void select_box(AdvectArgs& a, int box)
@@ -93,6 +95,7 @@ __device__ __forceinline__ void select_box(AdvectArgs& a, int box)
     a.uu = box_ptr(a.uu, a.bs.u, box);
     a.ub = box_ptr(a.ub, a.bs.b, box);
     a.dt_ptr = box_ptr(a.dt_ptr, a.bs.dt, box);
+    a.w = box_ptr(a.w, a.bs.w, box);
 }
 
 __device__ __forceinline__ void select_box(TransposeArgs& a, int box)
@@ -101,6 +104,7 @@ __device__ __forceinline__ void select_box(TransposeArgs& a, int box)
     a.b_out = box_ptr(a.b_out, a.bs.b, box);
     a.uu = box_ptr(a.uu, a.bs.u, box);
     a.ub = box_ptr(a.ub, a.bs.b, box);
+    a.w_out = box_ptr(a.w_out, a.bs.w, box);
 }
 
 template <typename R>
