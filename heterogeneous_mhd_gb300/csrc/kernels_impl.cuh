@@ -322,22 +322,22 @@ static bool plan_advect4(const AdvectArgs& a, bool aligned, A4Plan& p)
 
 // Persistent grid: the CTAs that fit on the device at once, shared among the
 // boxes of the launch, each with at least 8 chunks of work.
-template <int KT, int NS>
+template <int KT, int NS, bool WU = false>
 static cudaError_t launch_ad4(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
     static int per_sm = 0, nsm = 0;
-    cudaError_t e = allow_smem(k_advect4<EX, KT, NS>, attr, true);
+    cudaError_t e = allow_smem(k_advect4<EX, KT, NS, WU>, attr, true);
     if (e != cudaSuccess)
         return e;
-    const size_t smem = advect4_smem_bytes(KT, NS);
+    const size_t smem = advect4_smem_bytes(KT, NS, WU);
     if (!per_sm) {
         int dev = 0;
         e = cudaGetDevice(&dev);
         if (e == cudaSuccess)
             e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect4<EX, KT, NS>, advect4_threads(KT),
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect4<EX, KT, NS, WU>, advect4_threads(KT),
                                                               smem);
         if (e != cudaSuccess)
             return e;
@@ -350,12 +350,26 @@ static cudaError_t launch_ad4(const AdvectArgs& a, cudaStream_t s)
     if (ctas > cap)
         ctas = cap;
     dim3 grid((unsigned)ctas, 1, a.bs.count);
-    k_advect4<EX, KT, NS><<<grid, advect4_threads(KT), smem, s>>>(a);
+    k_advect4<EX, KT, NS, WU><<<grid, advect4_threads(KT), smem, s>>>(a);
     return cudaGetLastError();
 }
 
 static cudaError_t advect_x4(const AdvectArgs& a, const A4Plan& p, cudaStream_t s)
 {
+    // the (rho, m_x) side array of the fluidx before, when given, replaces u in the chunks
+    const bool wu = a.w != nullptr && (reinterpret_cast<uintptr_t>(a.w) & 15) == 0 &&
+                    (a.bs.count == 1 || a.bs.w % 16 == 0);
+    if (wu) {
+        switch (p.KT * 10 + p.NS) {
+        case 82: return launch_ad4<8, 2, true>(a, s);
+        case 83: return launch_ad4<8, 3, true>(a, s);
+        case 42: return launch_ad4<4, 2, true>(a, s);
+        case 43: return launch_ad4<4, 3, true>(a, s);
+        case 22: return launch_ad4<2, 2, true>(a, s);
+        case 23: return launch_ad4<2, 3, true>(a, s);
+        }
+        return cudaErrorInvalidValue;
+    }
     switch (p.KT * 10 + p.NS) {
     case 82: return launch_ad4<8, 2>(a, s);
     case 83: return launch_ad4<8, 3>(a, s);

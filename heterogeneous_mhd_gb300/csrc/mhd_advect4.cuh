@@ -38,16 +38,20 @@ constexpr int kA4X = 4;                  // cells per chunk
 constexpr int kA4J = 32;                 // pencils per tile along j
 constexpr int kA4UC = kA4J + 2;          // staged u columns j0-1..j0+32
 constexpr int kA4BC = kA4J + 1;          // staged b columns j0..j0+32
-constexpr int kA4UR = kA4UC * 5 * kA4X;  // floats of one staged u plane
 constexpr int kA4BR = kA4BC * 3 * kA4X;  // floats of one staged b plane
 
 __host__ __device__ inline int advect4_threads(int KT) { return (KT + 1) * 32; }
 
 // ring of NS (u, b) chunk buffers, then the EMF exchange: FB [KT+1][32] and
 // FA [KT] float4
-__host__ __device__ inline size_t advect4_smem_bytes(int KT, int NS)
+// staged u record of 4 cells in floats: the u records (20), or the (rho, m_x)
+// side array's (8, padded to 12 so that consecutive lanes read them with
+// 16-byte loads without bank conflicts)
+__host__ __device__ constexpr int advect4_urec(bool wu) { return wu ? 12 : 5 * kA4X; }
+
+__host__ __device__ inline size_t advect4_smem_bytes(int KT, int NS, bool wu = false)
 {
-    const size_t buf = (size_t)(KT + 2) * kA4UR + (size_t)(KT + 1) * kA4BR;
+    const size_t buf = (size_t)(KT + 2) * kA4UC * advect4_urec(wu) + (size_t)(KT + 1) * kA4BR;
     return (NS * buf + 4 * ((size_t)(KT + 1) * 32 + KT)) * sizeof(float);
 }
 
@@ -130,15 +134,25 @@ struct XRow {
     }
 };
 
-// rho and m_x (components 0, 1) of the four cells of a staged u record
+// rho and m_x (components 0, 1) of the four cells of a staged u record, or of
+// a side-array record (rho0, mx0, rho1, mx1, rho2, mx2, rho3, mx3)
+template <bool WU>
 __device__ __forceinline__ void a4_rho_mx(const float* p, float (&rho)[4], float (&mx)[4])
 {
     const float4* q = reinterpret_cast<const float4*>(p);
-    const float4 v0 = q[0], v1 = q[1], v2 = q[2], v3 = q[3], v4 = q[4];
-    rho[0] = v0.x, mx[0] = v0.y;
-    rho[1] = v1.y, mx[1] = v1.z;
-    rho[2] = v2.z, mx[2] = v2.w;
-    rho[3] = v3.w, mx[3] = v4.x;
+    if constexpr (WU) {
+        const float4 v0 = q[0], v1 = q[1];
+        rho[0] = v0.x, mx[0] = v0.y;
+        rho[1] = v0.z, mx[1] = v0.w;
+        rho[2] = v1.x, mx[2] = v1.y;
+        rho[3] = v1.z, mx[3] = v1.w;
+    } else {
+        const float4 v0 = q[0], v1 = q[1], v2 = q[2], v3 = q[3], v4 = q[4];
+        rho[0] = v0.x, mx[0] = v0.y;
+        rho[1] = v1.y, mx[1] = v1.z;
+        rho[2] = v2.z, mx[2] = v2.w;
+        rho[3] = v3.w, mx[3] = v4.x;
+    }
 }
 
 __device__ __forceinline__ void a4_b(const float* p, float (&b)[12])
@@ -168,17 +182,20 @@ __host__ __device__ constexpr int advect4_min_ctas(int KT, int NS)
     return KT == 2 ? 5 : (KT == 4 ? 3 : 1);
 }
 
-template <bool EX, int KT, int NS>
+// WU: the u chunks come from the (rho, m_x) side array a.w (8 bytes per cell)
+template <bool EX, int KT, int NS, bool WU = false>
 __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_advect4(AdvectArgs a)
 {
     static_assert(NS == 2 || NS == 3, "two or three chunk buffers");
     select_box(a, blockIdx.z);
     constexpr int NW = KT + 1;                            // warps
-    constexpr int UBUF = (KT + 2) * kA4UR, BBUF = (KT + 1) * kA4BR;
-    constexpr int UP = kA4UC * 5, BP = kA4BC * 3;        // 16-byte pieces of a staged plane: 170, 99
+    constexpr int REC = advect4_urec(WU), UR = kA4UC * REC;  // staged u record and plane (floats)
+    constexpr int UCELL = WU ? 2 : 5, PPR = WU ? 2 : 5;      // source floats per cell, 16-byte pieces per record
+    constexpr int UBUF = (KT + 2) * UR, BBUF = (KT + 1) * kA4BR;
+    constexpr int UP = kA4UC * PPR, BP = kA4BC * 3;          // 16-byte pieces of a staged plane
     constexpr int UQ = (UP + 31) / 32, BQ = (BP + 31) / 32;
     extern __shared__ __align__(16) float a4_smem[];
-    float* Us = a4_smem;                                  // [NS][KT+2][34][20]
+    float* Us = a4_smem;                                  // [NS][KT+2][34][REC]
     float* Bs = Us + NS * UBUF;                           // [NS][KT+1][33][12]
     float4* FBx = reinterpret_cast<float4*>(Bs + NS * BBUF);  // [KT+1][32]
     float4* FAx = FBx + NW * 32;                              // [KT]
@@ -189,6 +206,7 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
     const float dt = load_dt<float>(a.dt_ptr, a.dt_val);
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
+    const float* usrc = WU ? static_cast<const float*>(a.w) : uu;  // what the u chunks are staged from
     const float* b1s = static_cast<const float*>(a.b1_src);
     float* bo = static_cast<float*>(a.b_out);
     const bool b1_staged = (b1s == ub);
@@ -196,8 +214,8 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
     // this thread's rows: A at tile (ja, ka), B at (jb, kb); their staged records
     const int ja = bw ? kA4J : lane, ka = bw ? (lane < KT ? lane : 0) : w;
     const int jb = lane, kb = bw ? KT : w;
-    const int uAm = (ka + 1) * kA4UR + ja * 20, uAc = (ka + 1) * kA4UR + (ja + 1) * 20;
-    const int uBm = kb * kA4UR + (jb + 1) * 20, uBc = (kb + 1) * kA4UR + (jb + 1) * 20;
+    const int uAm = (ka + 1) * UR + ja * REC, uAc = (ka + 1) * UR + (ja + 1) * REC;
+    const int uBm = kb * UR + (jb + 1) * REC, uBc = (kb + 1) * UR + (jb + 1) * REC;
     const int bA = ka * kA4BR + ja * 12, bB = kb * kA4BR + jb * 12;
 
     // Work: whole tiles in rounds (CTA i takes tiles i, i + P, ...: all CTAs
@@ -234,10 +252,10 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
         int ucol[UQ], bcol[BQ];
 #pragma unroll
         for (int q = 0; q < UQ; q++) {
-            const int p = lane + 32 * q, c = p / 5, pc = p - 5 * c;
+            const int p = lane + 32 * q, c = p / PPR, pc = p - PPR * c;
             int jg = j0 + c - 1;
             jg = (jg < 0) ? jg + ny : (jg >= ny ? jg - ny : jg);
-            ucol[q] = (p < UP) ? jg * nx * 5 + pc * 4 : -1;
+            ucol[q] = (p < UP) ? jg * nx * UCELL + pc * 4 : -1;
         }
 #pragma unroll
         for (int q = 0; q < BQ; q++) {
@@ -247,25 +265,28 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
             bcol[q] = (p < BP) ? jg * nx * 3 + pc * 4 : -1;
         }
         auto kwrap = [&](int k) { return (k < 0) ? k + nz : (k >= nz ? k - nz : k); };
-        const int urow0 = kwrap(k0 + w - 1) * ny * nx * 5, urow1 = kwrap(k0 + KT) * ny * nx * 5;
+        const int urow0 = kwrap(k0 + w - 1) * ny * nx * UCELL, urow1 = kwrap(k0 + KT) * ny * nx * UCELL;
+        // shared offset of piece lane + 32 q of a staged plane: record p / PPR, piece p % PPR
+        const int ulane = WU ? ((lane >> 1) * REC + (lane & 1) * 4) : lane * 4;
+        constexpr int UQSTEP = WU ? 16 * REC : 128;
         const int brow = kwrap(k0 + w) * ny * nx * 3;
         // virtual chunk v (c0-1 .. c1, periodic) into ring buffer s
         auto load_chunk = [&](int v, int s) {
             const int xr = (v < 0) ? v + NC : (v >= NC ? v - NC : v);
-            float* ud0 = Us + s * UBUF + w * kA4UR + lane * 4;
+            float* ud0 = Us + s * UBUF + w * UR + ulane;
             float* bd0 = Bs + s * BBUF + w * kA4BR + lane * 4;
-            const float* us0 = uu + urow0 + xr * (5 * kA4X);
+            const float* us0 = usrc + urow0 + xr * (UCELL * kA4X);
 #pragma unroll
             for (int q = 0; q < UQ; q++)
                 if (ucol[q] >= 0)
-                    cp_async16(ud0 + 128 * q, us0 + ucol[q]);
+                    cp_async16(ud0 + UQSTEP * q, us0 + ucol[q]);
             if (w == 0) {  // the last staged u plane (k0 + KT)
-                float* ud1 = Us + s * UBUF + (KT + 1) * kA4UR + lane * 4;
-                const float* us1 = uu + urow1 + xr * (5 * kA4X);
+                float* ud1 = Us + s * UBUF + (KT + 1) * UR + ulane;
+                const float* us1 = usrc + urow1 + xr * (UCELL * kA4X);
 #pragma unroll
                 for (int q = 0; q < UQ; q++)
                     if (ucol[q] >= 0)
-                        cp_async16(ud1 + 128 * q, us1 + ucol[q]);
+                        cp_async16(ud1 + UQSTEP * q, us1 + ucol[q]);
             }
             const float* bs0 = ub + brow + xr * (3 * kA4X);
 #pragma unroll
@@ -301,9 +322,9 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
             float vxA[4], vxB[4], bvA[4], bvB[4], bd1[4];
             {
                 float rm[4], mm[4], rc[4], mc[4], rk[4], mk[4];
-                a4_rho_mx(U + uAm, rm, mm);
-                a4_rho_mx(U + uAc, rc, mc);
-                a4_rho_mx(U + uBm, rk, mk);
+                a4_rho_mx<WU>(U + uAm, rm, mm);
+                a4_rho_mx<WU>(U + uAc, rc, mc);
+                a4_rho_mx<WU>(U + uBm, rk, mk);
                 a4_face<EX>(rm, mm, rc, mc, vxA);
                 float ba[12];
                 a4_b(Bv + bA, ba);
@@ -317,7 +338,7 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
                     }
                 } else {
                     float rb[4], mb[4], bb[12];
-                    a4_rho_mx(U + uBc, rb, mb);
+                    a4_rho_mx<WU>(U + uBc, rb, mb);
                     a4_face<EX>(rk, mk, rb, mb, vxB);
                     a4_b(Bv + bB, bb);
 #pragma unroll
