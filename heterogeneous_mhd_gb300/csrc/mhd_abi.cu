@@ -109,7 +109,8 @@ struct mhd_ctx {
     DevBuf stage[4];    // drop-in host staging
     DevBuf alias[2];    // private copies of inputs that alias an output
     DevBuf divb;
-    DevBuf W;           // (rho, m_x) side array: x-sweep fluidx -> the advectbyzx after it (FP32)
+    DevBuf W;           // (rho, m_x) side array of the plain step (FP32): forward fluidx and backward
+                        // transposes write it, every advectbyzx reads it
     int* err_dev = nullptr;
     long long* nsteps_dev = nullptr;
     bool have_state = false;
