@@ -506,8 +506,20 @@ static cudaError_t calcfl(const void* u, const void* b, size_t ncell, void* part
     return cudaGetLastError();
 }
 
-static cudaError_t cfl_finalize(const CflFinalizeArgs& a, cudaStream_t s)
+static cudaError_t cfl_finalize(const CflFinalizeArgs& in, cudaStream_t s)
 {
+    CflFinalizeArgs a = in;
+    if (a.bs.count == 1 && a.scratch && a.nparts > kCflReduceMin) {
+        int g = (a.nparts + 511) / 512;
+        g = g < kCflReduceCtas ? g : kCflReduceCtas;
+        k_cfl_reduce<R><<<g, 256, 0, s>>>(static_cast<const CflPart<R>*>(a.part), a.nparts,
+                                          static_cast<CflPart<R>*>(a.scratch));
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+        a.part = a.scratch;
+        a.nparts = g;
+    }
     k_cfl_finalize<R, EX><<<a.bs.count, 1024, 0, s>>>(a);
     return cudaGetLastError();
 }

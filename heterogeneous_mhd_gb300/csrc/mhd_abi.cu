@@ -109,6 +109,7 @@ struct mhd_ctx {
     DevBuf stage[4];    // drop-in host staging
     DevBuf alias[2];    // private copies of inputs that alias an output
     DevBuf divb;
+    DevBuf cflred;      // first-level CFL reduction results (kCflReduceCtas partials)
     DevBuf W;           // (rho, m_x) side array of the plain step (FP32): forward fluidx and backward
                         // transposes write it, every advectbyzx reads it
     int* err_dev = nullptr;
@@ -406,7 +407,10 @@ static int op_finalize(mhd_ctx* c, int nparts, const void* u, const void* b, int
     a.clock = c->clock.p;
     a.nsteps = c->nsteps_dev;
     a.err = c->err_dev;
+    a.scratch = c->cflred.p;
     KTimer kt(c, MHD_K_FINALIZE);
+    if (a.scratch && nparts > kCflReduceMin)
+        c->launch_count++;  // the first-level reduction kernel
     CUDA_TRY(c->ks->cfl_finalize(a, c->stream));
     return MHD_OK;
 }
@@ -534,6 +538,7 @@ extern "C" MHD_API int mhd_set_state(mhd_ctx* c, const void* u, const void* b, i
         MHD_TRY(set_err(c->U[v].ensure(bu)));
         MHD_TRY(set_err(c->B[v].ensure(bb)));
     }
+    MHD_TRY(set_err(c->cflred.ensure((size_t)kCflReduceCtas * c->ks->part_bytes)));
     if (c->elem == 4)  // the side array of the plain step (allocated here: captured steps never allocate)
         MHD_TRY(set_err(c->W.ensure(ncell(c) * 2 * sizeof(float))));
     // CFL partials for both producers (standalone calcfl and the fluidx

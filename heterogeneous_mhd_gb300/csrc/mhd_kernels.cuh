@@ -126,6 +126,7 @@ struct CflFinalizeArgs {
     long long* nsteps;    // incremented when advance
     int* err;
     BoxStrides bs;        // batched: u, b and clock strides; nparts is per box
+    void* scratch;        // optional (one box): room for kCflReduceCtas CflPart<R> of a first-level reduction
 };
 
 // ------------------------------------------------------------- reductions
@@ -717,6 +718,44 @@ __global__ void __launch_bounds__(256) k_calcfl(const R* __restrict__ u, const R
 // c = max over cells after L (NaN if L is the last cell).  Then 1/c, and in
 // the time loop dt = cfl*(1/c) (double product as C/mhd.c:62), dt clamped to
 // (tf-t)/2 and t += 2dt (C/mhd.c:63-64).
+// First level of the CFL reduction over many partials: CTA g takes the
+// contiguous range g of the partials and writes their max speed and largest
+// NaN index (both order-free, so the result is the one-CTA reduction's).
+// One CTA reading 65536 partials is bound by its own L1 sector throughput.
+template <typename R>
+__global__ void __launch_bounds__(256) k_cfl_reduce(const CflPart<R>* __restrict__ part, int nparts,
+                                                    CflPart<R>* __restrict__ out)
+{
+    __shared__ R rm[8];
+    __shared__ int rn[8];
+    const int per = (nparts + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int s0 = (int)blockIdx.x * per, s1 = min(nparts, s0 + per);
+    R m = R(0);
+    int ln = -1;
+    for (int s = s0 + (int)threadIdx.x; s < s1; s += blockDim.x) {
+        m = fmax(m, part[s].cmax);
+        ln = max(ln, part[s].last_nan);
+    }
+    m = warp_max<R>(m);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        ln = max(ln, __shfl_xor_sync(0xffffffffu, ln, o));
+    if ((threadIdx.x & 31) == 0) {
+        rm[threadIdx.x >> 5] = m;
+        rn[threadIdx.x >> 5] = ln;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            m = fmax(m, rm[w]);
+            ln = max(ln, rn[w]);
+        }
+        out[blockIdx.x].cmax = m;
+        out[blockIdx.x].last_nan = ln;
+        out[blockIdx.x].pad = 0;
+    }
+}
+
 template <typename R, bool EX>
 __global__ void __launch_bounds__(1024) k_cfl_finalize(CflFinalizeArgs a)
 {

@@ -35,6 +35,11 @@ const KernelSet* kernels_f32_fast();
 const KernelSet* kernels_f32_exact();
 const KernelSet* kernels_f64_exact();
 
+// CFL finalize of one box: with more partials than kCflReduceMin a first
+// kernel of up to kCflReduceCtas CTAs reduces them into CflFinalizeArgs::scratch.
+constexpr int kCflReduceMin = 4096;
+constexpr int kCflReduceCtas = 128;
+
 // Pencils per CTA along j for fluidx / advectbyzx (a divisor of ny).
 int fluidx_pencils(int nx, int ny);
 int advect_pencils(int nx, int ny);
