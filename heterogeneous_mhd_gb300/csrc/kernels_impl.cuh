@@ -293,11 +293,13 @@ static cudaError_t advect_sweep(const AdvectArgs& a, const A3Plan& p3, cudaStrea
     return (p3.NS == 2) ? launch_ad3_t<8, 2, AX>(a, p3.T, s) : launch_ad3_t<8, 3, AX>(a, p3.T, s);
 }
 
-// x-walking kernel (FP32, the x sweep), chosen by the knob advect.kernel = 4
-// (the autotuner tries it; the marching kernel measured faster on GB300 at
-// 256^3, so it is not the planner's default): KT planes per CTA (4 by
-// default, or advect.xk), NS chunk buffers (2, or 3 by advect.slots); nx a
-// multiple of 4 and ny a multiple of 32.
+// x-walking kernel (FP32, the x sweep): the planner's choice for pencils
+// longer than 256 cells, where the marching kernel's rows would span more than
+// two warps (at 512^3 it measured 1.41 against 3.31 ms per launch), and by the
+// knob advect.kernel = 4 otherwise (the marching kernel measured faster at
+// 256^3).  KT planes per CTA (4 by default, or advect.xk), NS chunk buffers (2,
+// or 3 by advect.slots; 3 when the planner picks the kernel); nx a multiple of
+// 4 and ny a multiple of 32.
 struct A4Plan {
     int KT, NS;
 };
@@ -305,14 +307,16 @@ struct A4Plan {
 static bool plan_advect4(const AdvectArgs& a, bool aligned, A4Plan& p)
 {
     const int kn = tune_value(TUNE_ADVECT_KERNEL);
-    if (!kV2 || !aligned || a.axis != 0 || kn != 4)
+    const bool long_pencils = (kn == 0 && a.nx > 256);
+    if (!kV2 || !aligned || a.axis != 0 || !(kn == 4 || long_pencils))
         return false;
     if (a.nx % kA4X != 0 || a.ny % kA4J != 0)
         return false;
     if ((long long)a.nx * a.ny * a.nz * 5 >= (1LL << 31))  // 32-bit offsets inside a box
         return false;
     const int kt = tune_value(TUNE_ADVECT_XK);
-    p.NS = tune_value(TUNE_ADVECT_SLOTS) == 3 ? 3 : 2;
+    const int slots = tune_value(TUNE_ADVECT_SLOTS);
+    p.NS = (slots == 3 || (long_pencils && slots != 2)) ? 3 : 2;
     p.KT = 0;
     for (int k : {4, 8, 2})
         if (!p.KT && (kt == 0 || kt == k) && a.nz % k == 0)
