@@ -50,9 +50,9 @@ ALG_BYTES = {
     "fused": {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 64, "calcfl": 32, "copy": 64,
               "cfl_finalize": 0, "sweep": 64},
 }
-# per-cell bytes of a whole step in the survey's fixed convention (the
-# reference's operator sequence: 6 fluidx x 52 + 6 advectbyzx x 44 + 4
-# transposes x 64 + a calcfl 32), and what this step moves
+# per-cell bytes of a whole step in a fixed convention (the reference's
+# operator sequence: 6 fluidx x 52 + 6 advectbyzx x 44 + 4 transposes x 64 +
+# a calcfl 32), and what this step moves
 STEP_BYTES = {"plain": 864, "fused": 320}
 STEP_MOVED = {"plain": 6 * 52 + 3 * 8 + 6 * 32 + 4 * 64 + 2 * 8, "fused": 6 * 52 + 6 * 44}
 METRIC = "cell-updates/s at 256^3 (plain vs fused); closure speedup at matched error"
