@@ -146,12 +146,10 @@ def measured_traffic(kernel: str, n: int):
 def cpu_baseline(size: int, seconds: float = 12.0):
     """The oracle (the reference's C arithmetic) on this host's cores."""
     sys.path.insert(0, str(ROOT / "tests"))
-    from _oracle import REF, Oracle, strang_by_ops  # the checker, timed as the CPU baseline
+    from _oracle import Oracle  # the checker, timed as the CPU baseline
 
-    import heterogeneous_mhd_gb300 as mhd
-
-    u, b = mhd.init_turbulence(size, seed=0)
     port = Oracle(32, "port")
+    u, b = port.init_turbulence(size, seed=0)
     cores = port.max_threads()
     t0 = time.perf_counter()
     steps = 0
@@ -163,7 +161,7 @@ def cpu_baseline(size: int, seconds: float = 12.0):
     el = time.perf_counter() - t0
     # one core, as the reference's C path runs when built as shipped (64^3, a few seconds)
     port.set_threads(1)
-    u1, b1 = mhd.init_vortex(64, 64, 64, seed=0)
+    u1, b1 = port.init_vortex(64, 64, 64, seed=0)
     t1, steps1 = time.perf_counter(), 0
     while True:
         u1, b1, _, _, _ = port.strang(u1, b1, 64, 64, 64, 1)
@@ -184,13 +182,11 @@ def reference_arm(args):
     if rank != 0:
         return
     sys.path.insert(0, str(ROOT / "tests"))
-    from _oracle import REF, Oracle, strang_by_ops
-
-    import heterogeneous_mhd_gb300 as mhd
+    from _oracle import Oracle  # the CPU arm: nothing of the GPU library is loaded here
 
     n = args.size
-    u, b = mhd.init_turbulence(n, seed=0)
     kind, o = "port", Oracle(32, "port")
+    u, b = o.init_turbulence(n, seed=0)  # the same seeded box, from the C source built into the oracle
     cores = o.max_threads()
     for _ in range(args.warmup):
         u, b, _, _, _ = o.strang(u, b, n, n, n, 1)

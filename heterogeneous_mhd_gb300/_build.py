@@ -87,7 +87,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             jobs.append(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
                          "-fvisibility=hidden", "-I", str(ROOT / "include"), "-c", str(CSRC / csrc),
                          "-o", str(obj)])
-    with ThreadPoolExecutor(max_workers=4) as ex:
+    with ThreadPoolExecutor(max_workers=max(4, min(8, os.cpu_count() or 4))) as ex:
         list(ex.map(_run, jobs))
     objs = [OBJDIR / (u[0] + ".o") for u in units] + c_objs
     lib = lib_path()

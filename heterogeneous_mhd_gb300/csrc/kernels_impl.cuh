@@ -45,6 +45,9 @@ static cudaError_t allow_smem(K kernel, bool& done, bool tma_staged = false)
     return e;
 }
 
+// devices whose occupancy figures the persistent launchers cache
+constexpr int kMaxOccDevices = 64;
+
 static bool pow2_in(int T, int lo, int hi) { return T >= lo && T <= hi && (T & (T - 1)) == 0; }
 
 // ------------------------------------------------------------------ fluidx
@@ -330,16 +333,22 @@ template <int KT, int NS, bool WU = false>
 static cudaError_t launch_ad4(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    static int per_sm = 0, nsm = 0;
+    // occupancy per device (the process may drive several kinds of GPU)
+    static int per_sm_of[kMaxOccDevices] = {}, nsm_of[kMaxOccDevices] = {};
     cudaError_t e = allow_smem(k_advect4<EX, KT, NS, WU>, attr, true);
     if (e != cudaSuccess)
         return e;
     const size_t smem = advect4_smem_bytes(KT, NS, WU);
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= kMaxOccDevices)
+        return cudaErrorInvalidDevice;
+    int& per_sm = per_sm_of[dev];
+    int& nsm = nsm_of[dev];
     if (!per_sm) {
-        int dev = 0;
-        e = cudaGetDevice(&dev);
-        if (e == cudaSuccess)
-            e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect4<EX, KT, NS, WU>, advect4_threads(KT),
                                                               smem);

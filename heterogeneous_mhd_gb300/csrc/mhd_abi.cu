@@ -103,8 +103,12 @@ struct mhd_ctx {
     int device;
     cudaStream_t stream = nullptr;
     DevBuf U[2], B[2];  // ping-pong state; the current state is (U[0], B[0])
-    DevBuf part;        // CFL partials
+    DevBuf part;        // CFL partials of the step (the last fluidx's epilogue or ensure_cfl)
     DevBuf clock;       // R[4]: t, tf, dt, 1/c
+    DevBuf opart;       // partials of the standalone calcfl (mhd_op_calcfl, drop-in calcfl): never the
+                        // step's, so a standalone call neither changes the next step's dt nor
+                        // reallocates a buffer that a captured step graph reads
+    DevBuf opclock;     // result slot of the standalone calcfl (R[4]; only 1/c is written)
     DevBuf misc;        // err (int) + nsteps (long long) + divb partial scratch
     DevBuf stage[4];    // drop-in host staging
     DevBuf alias[2];    // private copies of inputs that alias an output
@@ -287,6 +291,10 @@ extern "C" MHD_API int mhd_destroy(mhd_ctx* c)
     }
     c->part.release();
     c->clock.release();
+    c->opart.release();
+    c->opclock.release();
+    c->cflred.release();
+    c->W.release();
     c->misc.release();
     c->divb.release();
     for (auto& s : c->stage)
@@ -359,12 +367,15 @@ static int op_advect(mhd_ctx* c, void* b_out, const void* b1_src, const void* uu
     return MHD_OK;
 }
 
+// transpose13 takes nx == nz (C/transpose13.c:50-61); `degenerate` also lets
+// nz == 1 or nx == 1 through, the two extra cases of the reference's CUDA
+// wrapper (Cuda/cuda_transpose13.cu:27-42), which the general kernel covers.
 static int op_transpose(mhd_ctx* c, int axis, void* u, void* b, const void* uu, const void* ub, int nx, int ny,
-                        int nz, void* w_out = nullptr)
+                        int nz, void* w_out = nullptr, bool degenerate = false)
 {
     if (nx <= 0 || ny <= 0 || nz <= 0)
         return MHD_ERR_ARG;
-    if (axis == 2 && nx != nz)
+    if (axis == 2 && nx != nz && !(degenerate && (nx == 1 || nz == 1)))
         return MHD_ERR_ARG;
     TransposeArgs a{u, b, uu, ub, nx, ny, nz, axis};
     a.w_out = w_out;
@@ -382,20 +393,22 @@ static int op_copy(mhd_ctx* c, const void* src, void* dst, size_t bytes)
     return MHD_OK;
 }
 
-// First CFL pass into c->part; returns the partial count in *np.
-static int op_calcfl_partials(mhd_ctx* c, const void* u, const void* b, size_t cells, int* np)
+// First CFL pass into `dst` (grown to fit); returns the partial count in *np.
+static int op_calcfl_partials(mhd_ctx* c, DevBuf& dst, const void* u, const void* b, size_t cells, int* np)
 {
-    MHD_TRY(c->part.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
+    MHD_TRY(dst.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
     KTimer kt(c, MHD_K_CALCFL);
-    CUDA_TRY(c->ks->calcfl(u, b, cells, c->part.p, np, BoxStrides{}, c->stream));
+    CUDA_TRY(c->ks->calcfl(u, b, cells, dst.p, np, BoxStrides{}, c->stream));
     return MHD_OK;
 }
 
-static int op_finalize(mhd_ctx* c, int nparts, const void* u, const void* b, int nx, int ny, int nz, double cfl,
-                       int advance)
+// Reduces `nparts` partials of `part` into the clock `clock` (advance: the
+// step's dt, clamp and t += 2 dt; otherwise only 1/c).
+static int op_finalize(mhd_ctx* c, const void* part, void* clock, int nparts, const void* u, const void* b, int nx,
+                       int ny, int nz, double cfl, int advance)
 {
     CflFinalizeArgs a{};
-    a.part = c->part.p;
+    a.part = part;
     a.nparts = nparts;
     a.u = u;
     a.b = b;
@@ -404,7 +417,7 @@ static int op_finalize(mhd_ctx* c, int nparts, const void* u, const void* b, int
     a.nz = nz;
     a.cfl = cfl;
     a.advance = advance;
-    a.clock = c->clock.p;
+    a.clock = clock;
     a.nsteps = c->nsteps_dev;
     a.err = c->err_dev;
     a.scratch = c->cflred.p;
@@ -481,16 +494,16 @@ extern "C" MHD_API int mhd_op_copy(mhd_ctx* c, const void* u, const void* b, voi
     return set_err(op_copy(c, b, ub, cells * 3 * c->elem));
 }
 
-static int read_clock(mhd_ctx* c, double out[4])
+static int read_clock(mhd_ctx* c, const void* clock, double out[4])
 {
     if (c->elem == 4) {
         float h[4];
-        CUDA_TRY(cudaMemcpyAsync(h, c->clock.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(h, clock, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(cudaStreamSynchronize(c->stream));
         for (int s = 0; s < 4; s++)
             out[s] = h[s];
     } else {
-        CUDA_TRY(cudaMemcpyAsync(out, c->clock.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(out, clock, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(cudaStreamSynchronize(c->stream));
     }
     return MHD_OK;
@@ -504,10 +517,11 @@ static int calcfl_sync(mhd_ctx* c, const void* u, const void* b, int nx, int ny,
         return MHD_OK;
     }
     int np = 0;
-    MHD_TRY(op_calcfl_partials(c, u, b, cells, &np));
-    MHD_TRY(op_finalize(c, np, u, b, nx, ny, nz, 0.0, 0));
+    MHD_TRY(c->opclock.ensure(4 * sizeof(double)));
+    MHD_TRY(op_calcfl_partials(c, c->opart, u, b, cells, &np));
+    MHD_TRY(op_finalize(c, c->opart.p, c->opclock.p, np, u, b, nx, ny, nz, 0.0, 0));
     double clk[4];
-    MHD_TRY(read_clock(c, clk));
+    MHD_TRY(read_clock(c, c->opclock.p, clk));
     *inv = clk[3];
     int herr = 0;
     CUDA_TRY(cudaMemcpy(&herr, c->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
@@ -615,7 +629,7 @@ extern "C" MHD_API int mhd_get_time(mhd_ctx* c, double* t, double* dt, long long
     if (!c)
         return set_err(MHD_ERR_ARG);
     double clk[4];
-    MHD_TRY(set_err(read_clock(c, clk)));
+    MHD_TRY(set_err(read_clock(c, c->clock.p, clk)));
     if (t)
         *t = clk[0];
     if (dt)
@@ -644,7 +658,7 @@ static int enqueue_plain_step(mhd_ctx* c, double cfl)
         const bool al = ((size_t)ax * 5 * c->elem) % 16 == 0 && ((size_t)ax * 3 * c->elem) % 16 == 0;
         return (c->W.p && c->ks->fluidx_writes_w(ax, ay, az, al ? 1 : 0)) ? c->W.p : nullptr;
     };
-    MHD_TRY(op_finalize(c, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
+    MHD_TRY(op_finalize(c, c->part.p, c->clock.p, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
     // x sweep
     void* W = side(nx, ny, nz);
     MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 0, W));
@@ -692,7 +706,7 @@ static int enqueue_fused_step(mhd_ctx* c, double cfl)
     const int nx = c->nx, ny = c->ny, nz = c->nz;
     void *U0 = c->U[0].p, *U1 = c->U[1].p, *B0 = c->B[0].p, *B1 = c->B[1].p;
     const void* dt = static_cast<char*>(c->clock.p) + 2 * c->elem;
-    MHD_TRY(op_finalize(c, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
+    MHD_TRY(op_finalize(c, c->part.p, c->clock.p, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
     // x
     MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 0));
     MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 0));
@@ -727,9 +741,8 @@ static int ensure_cfl(mhd_ctx* c)
     if (c->cfl_valid)
         return MHD_OK;
     const size_t cells = ncell(c);
-    MHD_TRY(c->part.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
     int np = 0;
-    MHD_TRY(op_calcfl_partials(c, c->U[0].p, c->B[0].p, cells, &np));
+    MHD_TRY(op_calcfl_partials(c, c->part, c->U[0].p, c->B[0].p, cells, &np));
     c->cfl_nparts = np;
     c->cfl_valid = true;
     return MHD_OK;
@@ -1415,12 +1428,18 @@ static void cuda_transpose(int axis, float* ut, float* bt, float* u, float* b, c
     mhd_ctx* c;
     if (set_err(dropin_ctx(&c)) != MHD_OK)
         return;
-    if (set_err(op_transpose(c, axis, ut, bt, u, b, *h_nx, *h_ny, *h_nz)) != MHD_OK)
+    if (set_err(op_transpose(c, axis, ut, bt, u, b, *h_nx, *h_ny, *h_nz, nullptr, true)) != MHD_OK)
+        return;
+    // like the reference's wrappers (Cuda/cuda_transpose12.cu:30-34), the
+    // transposed state is copied back, so u and b hold it on return as well
+    const size_t cells = (size_t)(*h_nx) * (*h_ny) * (*h_nz);
+    if (set_err(op_copy(c, ut, u, cells * 5 * sizeof(float))) != MHD_OK ||
+        set_err(op_copy(c, bt, b, cells * 3 * sizeof(float))) != MHD_OK)
         return;
     set_err(cudaStreamSynchronize(c->stream) == cudaSuccess ? MHD_OK : MHD_ERR_CUDA);
 }
 
-// (ut, bt) <- transpose12(u, b) (Cuda/cuda_transpose12.cu)
+// (ut, bt) <- transpose12(u, b), then (u, b) <- (ut, bt) (Cuda/cuda_transpose12.cu:12-38)
 extern "C" MHD_API void cuda_transpose12(float* ut, float* bt, float* u, float* b, int* nx, int* ny, int* nz,
                                          int* h_nx, int* h_ny, int* h_nz)
 {
@@ -1428,7 +1447,8 @@ extern "C" MHD_API void cuda_transpose12(float* ut, float* bt, float* u, float* 
     cuda_transpose(1, ut, bt, u, b, h_nx, h_ny, h_nz);
 }
 
-// (ut, bt) <- transpose13(u, b), nx == nz (Cuda/cuda_transpose13.cu)
+// (ut, bt) <- transpose13(u, b), then (u, b) <- (ut, bt); nx == nz, nz == 1 or nx == 1
+// (Cuda/cuda_transpose13.cu:14-55)
 extern "C" MHD_API void cuda_transpose13(float* ut, float* bt, float* u, float* b, int* nx, int* ny, int* nz,
                                          int* h_nx, int* h_ny, int* h_nz)
 {

@@ -74,7 +74,10 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
             tma_load_1d(sbk, ub + ck * 3, bg, &bar);
         }
         __syncthreads();
-        mbar_wait_bounded(&bar, 0, a.err);
+        // a copy that never lands (the wait gave up and set the error bit):
+        // the whole CTA leaves before computing on unfilled shared memory
+        if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
+            return;
     } else {
         // rows of P cells (x0..x0+P-1) at plane k and k+1, and the b of x0+P;
         // consecutive threads read consecutive words of a row

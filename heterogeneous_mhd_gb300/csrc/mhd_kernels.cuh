@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(512) k_fluidx(FluidxArgs a)
             tma_load_1d(sbk, ub + ck * 3, bg, &bar);
         }
         __syncthreads();
-        mbar_wait_bounded(&bar, 0, a.err);
+        if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
+            return;  // the copy never landed (error bit set): leave before computing on it
     } else {
         coop_copy(su, uu + c0 * 5, (size_t)5 * np);
         coop_copy(sb, ub + c0 * 3, (size_t)3 * np);

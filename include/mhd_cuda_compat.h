@@ -10,8 +10,10 @@
  *   cuda_cfl          *h_dt = 1/max speed (also copied to dt on the device)
  *   cuda_fluidx       u <- fluidx(u, b) in place, dt read on the device
  *   cuda_advectbyzx   b <- advectbyzx(u, b) in place; temp is not used
- *   cuda_transpose12  (ut, bt) <- transpose12(u, b)
- *   cuda_transpose13  (ut, bt) <- transpose13(u, b), nx == nz
+ *   cuda_transpose12  (ut, bt) <- transpose12(u, b), then (u, b) <- (ut, bt)
+ *   cuda_transpose13  (ut, bt) <- transpose13(u, b), then (u, b) <- (ut, bt);
+ *                     nx == nz, or the degenerate nz == 1 / nx == 1 boxes
+ *                     (Cuda/cuda_transpose13.cu:27-42)
  */
 #ifndef MHD_CUDA_COMPAT_H
 #define MHD_CUDA_COMPAT_H

@@ -207,10 +207,13 @@ MHD_API int mhd_divb_max(mhd_ctx *ctx, double *out);
  * scratch is a fixed file-scope device array (768 KB per device, held until the
  * process exits).  u, b and inv_cmax are device pointers; the two kernels are
  * queued on `stream` (a cudaStream_t, NULL for the default stream) and
- * *inv_cmax is written when the stream reaches them.  Grids of more than
- * 134,217,728 cells (512^3) return MHD_ERR_UNSUPPORTED.  The first call on a
- * device looks up the array's address and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * *inv_cmax is written when the stream reaches them.  It always computes with
+ * the FAST arithmetic (FP32 with contraction), whatever MHD_GB300_MODE or a
+ * context's flags say.  Grids of more than 134,217,728 cells (512^3) return
+ * MHD_ERR_UNSUPPORTED.  The first call on a device looks up the array's
+ * address and should come before any stream capture; the address is kept for
+ * the life of the process, so calling it after cudaDeviceReset is not
+ * supported.  All calls share the array: calls that overlap on the GPU race. */
 MHD_API int mhd_calcfl_noalloc(const float *u, const float *b, int nx, int ny, int nz, float *inv_cmax,
                                void *stream);
 

@@ -54,6 +54,12 @@ class Oracle:
             fn.argtypes = args
             self._f[name] = fn
         if kind == "port":
+            L.mhd_init_turbulence.restype = C.c_int
+            L.mhd_init_turbulence.argtypes = [vp, vp, C.c_int, C.c_int, C.c_ulonglong, C.c_double, C.c_double,
+                                              C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
+            L.mhd_init_vortex.restype = C.c_int
+            L.mhd_init_vortex.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.c_double,
+                                          C.c_double, C.c_double, C.c_double, C.c_double]
             L.orc_strang_steps.restype = C.c_int
             L.orc_strang_steps.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                            real, rp, rp]
@@ -88,6 +94,25 @@ class Oracle:
 
     def calcfl(self, u, b, nx, ny, nz):
         return float(self._f["calcfl"](self._a(u), self._a(b), *self._d(nx, ny, nz)))
+
+    def init_turbulence(self, n, seed=0, rho0=1.0, p0=1.0, mach=0.5, bx0=0.3, dbrms=0.1, kmin=2, kmax=8):
+        """The package's seeded turbulence box (the same C source as
+        heterogeneous_mhd_gb300.init_turbulence), built into the oracle so a
+        CPU-only run needs no GPU library."""
+        u = np.empty(5 * n ** 3, dtype=self.dtype)
+        b = np.empty(3 * n ** 3, dtype=self.dtype)
+        st = self._L.mhd_init_turbulence(self._a(u), self._a(b), n, int(self.dtype == np.float64), seed, rho0, p0,
+                                         mach, bx0, dbrms, kmin, kmax)
+        assert st == 0, st
+        return u, b
+
+    def init_vortex(self, nx, ny, nz, seed=0, rho0=1.0, p0=0.6, vscale=1.0, noise=1e-3, bscale=1.0):
+        u = np.empty(5 * nx * ny * nz, dtype=self.dtype)
+        b = np.empty(3 * nx * ny * nz, dtype=self.dtype)
+        st = self._L.mhd_init_vortex(self._a(u), self._a(b), nx, ny, nz, int(self.dtype == np.float64), seed, rho0,
+                                     p0, vscale, noise, bscale)
+        assert st == 0, st
+        return u, b
 
     def set_threads(self, n: int) -> None:
         if self.kind == "port":
@@ -148,5 +173,12 @@ def strang_by_ops(o, u, b, nx, ny, nz, nsteps, cfl=0.7, tf=float("inf"), t=0.0):
     return u, b, float(t), float(dt), s
 
 
+def ref_src() -> str:
+    """Directory of the reference's C/ sources named by MHD_REF_SRC ('' if none)."""
+    import os
+    d = os.environ.get("MHD_REF_SRC", "")
+    return d if d and Path(d).is_dir() else ""
+
+
 def have_ref() -> bool:
-    return REF[32].exists() or (Path("/root/reference/C").is_dir())
+    return REF[32].exists() or bool(ref_src())

@@ -1,8 +1,9 @@
 """Generate the golden fixtures from the reference's own C/ sources.
 
-Run in the development container, where /root/reference exists:
+Run in the development container, with MHD_REF_SRC naming the reference's
+C/ directory:
 
-    python tests/golden/make_golden.py
+    MHD_REF_SRC=/root/reference/C python tests/golden/make_golden.py
 
 It builds oracle/_ref (the reference's C/ files compiled in place by
 oracle/Makefile), runs them on seeded inputs and writes

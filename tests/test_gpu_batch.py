@@ -137,3 +137,32 @@ def test_batch_x_walking_advect_exact_vs_oracle(mhd, cuda, oracle32):
                 assert bitwise_equal(u, ou) and bitwise_equal(b, ob), (i, box)
     finally:
         autotune.apply({})
+
+
+@pytest.mark.slow
+def test_batch_large_classes_vs_oracle(mhd, cuda, oracle32):
+    """The benched workload's two largest size classes (96^3 and 128^3 boxes,
+    two of each with their own beta and Mach) inside a batch that also holds
+    the smaller classes: sampled boxes bit for bit against the oracle with the
+    EXACT kernels, and within the FAST one-step tolerance per field after one
+    step with the production kernels."""
+    from util import rel_l2_fields
+    cfg = mhd.batch_config(10, seed=17)
+    for x, n in zip(cfg, (96, 128, 96, 128, 32, 48, 64, 32, 48, 64)):
+        x["n"] = n
+    sample = [0, 1, 2, 3]
+    for exact, nsteps in ((True, 2), (False, 1)):
+        bt, ics = make_batch(mhd, cfg, exact=exact)
+        with bt:
+            bt.step(nsteps)
+            bt.sync()
+            for i in sample:
+                n = cfg[i]["n"]
+                u, b = bt.get_box(i)
+                ou, ob, ot, _, _ = oracle32.strang(*ics[i], n, n, n, nsteps, 0.7)
+                if exact:
+                    assert bitwise_equal(u, ou) and bitwise_equal(b, ob), (i, cfg[i])
+                    assert np.float32(bt.time(i)[0]) == np.float32(ot)
+                else:
+                    e = rel_l2_fields(u, b, ou, ob)
+                    assert max(e.values()) <= 1e-5, (i, e)

@@ -149,6 +149,34 @@ def test_x_walking_advect_vs_oracle(shape, mhd, cuda, oracle32):
     assert tried > 0
 
 
+@pytest.mark.parametrize("shape", [(288, 32, 4), (512, 32, 4)])
+def test_default_advect_long_pencils_vs_oracle(shape, mhd, cuda, oracle32):
+    """Pencils longer than 256 cells take the x-walking advectbyzx by the
+    planner's default (no knob set): EXACT bit for bit against the oracle and
+    FAST within the operator tolerance, so the 512^3 production path is pinned
+    to the reference independently of the FAST-vs-EXACT comparison."""
+    from heterogeneous_mhd_gb300 import autotune
+    torch = cuda
+    nx, ny, nz = shape
+    autotune.apply({})
+    u, b = mhd.init_vortex(nx, ny, nz, seed=nx + nz)
+    rng = np.random.default_rng(nx)
+    b = (b + 0.05 * rng.standard_normal(b.shape)).astype(np.float32)
+    bin_ = (b * np.float32(0.75)).astype(np.float32)
+    ref = bin_.copy()
+    oracle32.advectbyzx(u.copy(), ref, nx, ny, nz, DT, u.copy(), b.copy())
+    for exact in (True, False):
+        with mhd.Context(1, 1, 1, exact=exact) as ctx:
+            bo = dev(torch, bin_)
+            ctx.op_advectbyzx(bo, dev(torch, u), dev(torch, b), nx, ny, nz, DT)
+            ctx.sync()
+            got = host(bo)
+        if exact:
+            assert bitwise_equal(got, ref), shape
+        else:
+            assert rel_l2(got, ref) < FAST_OP_TOL, shape
+
+
 def test_in_place_and_aliased_arguments(mhd, cuda, oracle32):
     """The reference's C/ allows u == update_u for fluidx and b == update_b for
     advectbyzx and the transposes (it works pencil by pencil / plane by plane);

@@ -123,3 +123,35 @@ def test_run_driver_log_checkpoint_and_resume(mhd, cuda, tmp_path):
     assert more[-1]["step"] == straight[-1]["step"] == 8
     for key in ("t", "dt", "min_rho", "min_p", "max_divb", "mass", "kinetic", "magnetic", "energy", "max_speed"):
         assert more[-1][key] == straight[-1][key], key
+
+
+def test_standalone_calcfl_between_steps_changes_nothing(mhd, cuda):
+    """mhd_op_calcfl on other (and larger) arrays between two steps of a
+    context keeps its own scratch: the steps after it are bit for bit those of
+    an uninterrupted run, with graphs and with direct launches."""
+    torch = cuda
+    n = 32
+    u0, b0 = mhd.init_turbulence(n, seed=6)
+    ub, bb = mhd.init_vortex(96, 96, 96, seed=7, vscale=3.0)
+    du, db = torch.from_numpy(ub).cuda(), torch.from_numpy(bb).cuda()
+    for graphs in (True, False):
+        with mhd.Context(n, n, n) as ref:
+            ref.use_graphs(graphs)
+            ref.set_state(u0, b0)
+            ref.step(3)
+            ru, rb = ref.get_state()
+            rt = ref.time()
+        with mhd.Context(n, n, n) as ctx:
+            ctx.use_graphs(graphs)
+            ctx.set_state(u0, b0)
+            ctx.step(1)
+            inv = ctx.op_calcfl(du, db, 96, 96, 96)
+            assert np.isfinite(inv) and inv > 0
+            ctx.step(1)
+            ctx.op_calcfl(du, db, 96, 96, 96)
+            ctx.step(1)
+            u, b = ctx.get_state()
+            t = ctx.time()
+            assert ctx.check() == mhd.MHD_OK
+        assert bitwise_equal(u, ru) and bitwise_equal(b, rb), graphs
+        assert t == rt
