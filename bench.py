@@ -39,21 +39,23 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# algorithmic HBM bytes per cell of one launch of each kernel, averaged over
-# the launches of a step (FP32 AoS: u 20 B, b 12 B per cell).  Plain step:
-# the three forward fluidx launches and the two backward transposes also write
-# the (rho, m_x) side array (8 B), and every advectbyzx reads it in place of u
-# (8 B instead of 20).  Fused step: no side array.
-ALG_BYTES = {
-    "plain": {"fluidx": 52 + 8 * 3 / 6, "advectbyzx": 32, "transpose12": 64 + 8 / 2, "transpose13": 64 + 8 / 2,
-              "calcfl": 32, "copy": 64, "cfl_finalize": 0, "sweep": 64},
-    "fused": {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 64, "calcfl": 32, "copy": 64,
-              "cfl_finalize": 0, "sweep": 64},
-}
-# per-cell bytes of a whole step in a fixed convention (the reference's
-# operator sequence: 6 fluidx x 52 + 6 advectbyzx x 44 + 4 transposes x 64 +
-# a calcfl 32), and what this step moves
-STEP_BYTES = {"plain": 864, "fused": 320}
+# Algorithmic HBM bytes per cell of one launch of each kernel, FP32 AoS (u 20
+# B, b 12 B per cell), in the fixed convention of the reference's operators:
+# fluidx reads u and b and writes u (52), advectbyzx reads u and b and writes
+# b (44), a transpose reads and writes the state (64), calcfl reads it (32).
+ALG_BYTES = {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 64, "calcfl": 32, "copy": 64,
+             "cfl_finalize": 0, "sweep": 64}
+# What the plain step's kernels move on average per launch: the three forward
+# fluidx launches and the two backward transposes also write the (rho, m_x)
+# side array (8 B), and every advectbyzx reads it in place of u (8 B, not 20).
+MOVED_BYTES = {"plain": {"fluidx": 52 + 8 * 3 / 6, "advectbyzx": 32, "transpose12": 64 + 8 / 2,
+                         "transpose13": 64 + 8 / 2},
+               "fused": {"fluidx": 52, "advectbyzx": 44}}
+# per-cell bytes of a whole step: the reference's operator sequence (6 fluidx
+# x 52 + 6 advectbyzx x 44 + 4 transposes x 64 + a calcfl 32 = 864), what the
+# fused step's operators move (no transposes: 6 x 52 + 6 x 44 = 576), and the
+# five-pass bound of a step that fuses each sweep's operators (5 x 64 = 320)
+STEP_BYTES = {"plain": 864, "fused": 576, "fused_5pass": 320}
 STEP_MOVED = {"plain": 6 * 52 + 3 * 8 + 6 * 32 + 4 * 64 + 2 * 8, "fused": 6 * 52 + 6 * 44}
 METRIC = "cell-updates/s at 256^3 (plain vs fused); closure speedup at matched error"
 
@@ -130,7 +132,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def measured_traffic(kernel: str, n: int):
+def measured_traffic(kernel: str, n: int, variant: str = "plain"):
     """DRAM bytes per launch of `kernel` from the committed ncu capture
     (profiles/traffic_256.json) when it was taken on this grid, else None."""
     p = ROOT / "profiles" / "traffic_256.json"
@@ -138,6 +140,7 @@ def measured_traffic(kernel: str, n: int):
         t = json.loads(p.read_text())
     except (OSError, ValueError):
         return None
+    t = t.get(variant, t) if variant in t else (t if variant == "plain" else {})
     if t.get("grid") != [n, n, n] or kernel not in t:
         return None
     return t[kernel]["dram_bytes_per_launch"]
@@ -290,6 +293,94 @@ def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3):
     return out
 
 
+def time_steps(ctx, stream, torch, barrier, steps: int, fused: bool):
+    """Graph-replay steps timed with CUDA events on the library's stream, and
+    the same steps launched directly with an event pair around every kernel
+    (per-kernel times).  Returns (ms, launches, ms_profiled, kernels)."""
+    import heterogeneous_mhd_gb300 as mhd
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    l0 = ctx.launch_count()
+    ev0.record(stream)
+    ctx.step(steps, cfl=0.7, fused=fused)
+    ev1.record(stream)
+    ev1.synchronize()
+    barrier()
+    launches = ctx.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    ctx.profile(True)
+    ctx.profile_reset()
+    barrier()
+    ev0.record(stream)
+    ctx.step(steps, cfl=0.7, fused=fused)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms_prof = ev0.elapsed_time(ev1)
+    kern = {k: ctx.profile_read(k) for k in mhd.KERNELS}
+    ctx.profile(False)
+    return ms, launches, ms_prof, kern
+
+
+def variant_summary(variant: str, cells: int, steps: int, ms: float, kern: dict, hbm: float, n: int):
+    """Throughput, step bandwidth in the fixed conventions and the roofline of
+    the dominant kernel of one step variant."""
+    sec = ms / steps * 1e-3
+    out = {"ms_per_step": ms / steps, "value": cells / sec, "unit": "cell-updates/s"}
+    out["step_alg_bytes_per_cell"] = STEP_BYTES[variant]
+    out["step_alg_gbs"] = STEP_BYTES[variant] * cells / sec / 1e9
+    out["step_frac"] = out["step_alg_gbs"] / hbm
+    out["step_moved_bytes_per_cell"] = STEP_MOVED[variant]
+    out["step_moved_frac"] = STEP_MOVED[variant] * cells / sec / 1e9 / hbm
+    if variant == "fused":  # the five-pass bound of a fully fused sweep
+        out["step_frac_5pass_320"] = STEP_BYTES["fused_5pass"] * cells / sec / 1e9 / hbm
+    if kern:
+        dom = max((k for k in kern if kern[k][1] > 0), key=lambda k: kern[k][0])
+        tot_ms, nl = kern[dom]
+        mean_ms = tot_ms / nl
+        alg = ALG_BYTES[dom]
+        achieved = alg * cells / (mean_ms * 1e-3) / 1e9
+        moved = MOVED_BYTES.get(variant, {}).get(dom, alg)
+        total = sum(x[0] for x in kern.values())
+        out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                           "frac": achieved / hbm, "alg_bytes_per_cell": alg, "alg_bytes_per_launch": alg * cells,
+                           "mean_launch_ms": mean_ms, "traffic": measured_traffic(dom, n, variant),
+                           "moved_bytes_per_cell": moved,
+                           "frac_moved": moved * cells / (mean_ms * 1e-3) / 1e9 / hbm}
+        out["kernels"] = {k: {"ms_total": round(v[0], 4), "launches": v[1], "share": round(v[0] / total, 4),
+                              "mean_us": round(1e3 * v[0] / v[1], 2),
+                              "frac": round(ALG_BYTES[k] * cells / (v[0] / v[1] * 1e-3) / 1e9 / hbm, 4)
+                              if ALG_BYTES.get(k) else None}
+                          for k, v in kern.items() if v[1] > 0}
+    return out
+
+
+def size512_leg(mhd, torch, steps=5, warmup=3):
+    """Config 2's second grid: the plain step at 512^3 (4.3 GB of state),
+    graph replay timed with CUDA events."""
+    n = 512
+    cells = n ** 3
+    u0, b0 = mhd.init_turbulence(n, seed=0)
+    hbm, _ = peaks()
+    with mhd.Context(n, n, n) as ctx:
+        ctx.set_state(u0, b0)
+        del u0, b0
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        ctx.step(warmup, cfl=0.7)
+        ctx.sync()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        ctx.step(steps, cfl=0.7)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        status = ctx.check()
+    out = {"workload": "decaying turbulence 512^3, FP32, CFL 0.7, plain Strang step", "grid": [n, n, n],
+           "steps": steps, "status": int(status)}
+    out.update(variant_summary("plain", cells, steps, ms, {}, hbm, n))
+    return out
+
+
 def our_arm(args):
     import torch
 
@@ -310,49 +401,32 @@ def our_arm(args):
     ctx = mhd.Context(n, n, n)
     ctx.set_state(u0, b0)
     stream = torch.cuda.ExternalStream(ctx.stream())
-    fused = args.variant == "fused"
+    main = args.variant
+    other = "plain" if main == "fused" else "fused"
+    hbm, src = peaks()
 
     def barrier():
         ctx.sync()
         torch.cuda.synchronize()
         rep.barrier()
 
-    # warm-up (also captures the step graph), then one step through the
-    # profiled direct-launch path so the timed region starts warm on it too
-    ctx.step(args.warmup, cfl=0.7, fused=fused)
-    ctx.profile(True)
-    ctx.step(1, cfl=0.7, fused=fused)
-    ctx.profile(False)
+    # warm-up of both variants (captures their step graphs), then one step of
+    # each through the profiled direct-launch path
+    for v in (main, other):
+        ctx.step(args.warmup, cfl=0.7, fused=(v == "fused"))
+        ctx.profile(True)
+        ctx.step(1, cfl=0.7, fused=(v == "fused"))
+        ctx.profile(False)
     barrier()
 
-    # timed region: the production path, one CUDA graph replay per step
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # timed region: the production path of the headline variant, one CUDA graph replay per step
     with ClockSampler(torch.cuda.current_device()) as clk:
-        barrier()
-        l0 = ctx.launch_count()
-        ev0.record(stream)
-        ctx.step(args.steps, cfl=0.7, fused=fused)
-        ev1.record(stream)
-        ev1.synchronize()
-        barrier()
-        launches = ctx.launch_count() - l0
-        ms = ev0.elapsed_time(ev1)
-
-        # the same steps launched directly with an event pair around every
-        # kernel: per-kernel durations for the roofline
-        ctx.profile(True)
-        ctx.profile_reset()
-        barrier()
-        ev0.record(stream)
-        ctx.step(args.steps, cfl=0.7, fused=fused)
-        ev1.record(stream)
-        ev1.synchronize()
-        ms_profiled = ev0.elapsed_time(ev1)
-        kern = {k: ctx.profile_read(k) for k in mhd.KERNELS}
-        ctx.profile(False)
+        ms, launches, ms_profiled, kern = time_steps(ctx, stream, torch, barrier, args.steps, main == "fused")
+        ms_o, launches_o, ms_profiled_o, kern_o = time_steps(ctx, stream, torch, barrier, args.steps,
+                                                             other == "fused")
         status = ctx.check()
-
     value, t_max = rep.throughput(cells, args.steps, ms)
+    value_o, _ = rep.throughput(cells, args.steps, ms_o)
 
     # e2e: host state in and out of the C ABI every step
     hu = torch.empty(5 * cells, dtype=torch.float32, pin_memory=True)
@@ -364,50 +438,52 @@ def our_arm(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx.set_state(hu, hb)   # H2D from pinned memory
-        ctx.step(1, cfl=0.7, fused=fused)
+        ctx.step(1, cfl=0.7, fused=(main == "fused"))
         ctx.get_state_into(hu, hb)  # D2H, synchronises
     e2e_s = time.perf_counter() - t0
     (e2e_s,) = rep.max([e2e_s])
     e2e = world * cells * e2e_steps / e2e_s
-
-    # roofline of the dominant kernel
-    hbm, src = peaks()
-    dom = max((k for k in kern if kern[k][1] > 0), key=lambda k: kern[k][0])
-    traffic = measured_traffic(dom, n)
-    tot_ms, nl = kern[dom]
-    mean_ms = tot_ms / nl
-    alg = ALG_BYTES[args.variant][dom]
-    achieved = alg * cells / (mean_ms * 1e-3) / 1e9
-    step_bw = STEP_BYTES[args.variant] * cells / (ms / args.steps * 1e-3) / 1e9
-    moved_bw = STEP_MOVED[args.variant] * cells / (ms / args.steps * 1e-3) / 1e9
     if rank != 0:
         ctx.close()
         rep.close()
         return
-    share = {k: round(v[0] / sum(x[0] for x in kern.values()), 4) for k, v in kern.items() if v[1] > 0}
+
+    head = variant_summary(main, cells, args.steps, ms, kern, hbm, n)
+    sub = variant_summary(other, cells, args.steps, ms_o, kern_o, hbm, n)
+    sub.update({"value": value_o, "gpu_launches": int(launches_o), "profiled_ms_per_step": ms_profiled_o / args.steps})
+    roof = head["roofline"]
+    roof["peak_source"] = src
+    roof.update({"step_alg_gbs": head["step_alg_gbs"], "step_frac": head["step_frac"],
+                 "step_alg_bytes_per_cell": head["step_alg_bytes_per_cell"],
+                 "step_moved_bytes_per_cell": head["step_moved_bytes_per_cell"],
+                 "step_moved_frac": head["step_moved_frac"]})
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"decaying turbulence {n}^3, FP32, CFL 0.7, {args.variant} Strang step",
-                   "grid": [n, n, n], "variant": args.variant, "parallelism": "replicas" if world > 1 else "single",
+        "config": {"workload": f"decaying turbulence {n}^3, FP32, CFL 0.7, {main} Strang step",
+                   "grid": [n, n, n], "variant": main, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "state 537 MB > L2, no flush", "launch_shapes": tuned or "planner defaults"},
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": 32 * cells,
                 "d2h_bytes_per_step": 32 * cells, "steps": e2e_steps},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
-                     "alg_bytes_per_launch": alg * cells, "mean_launch_ms": mean_ms,
-                     "step_alg_gbs": step_bw, "step_frac": step_bw / hbm,
-                     "step_moved_bytes_per_cell": STEP_MOVED[args.variant], "step_moved_gbs": moved_bw,
-                     "step_moved_frac": moved_bw / hbm},
-        "kernels": {k: {"ms_total": round(v[0], 4), "launches": v[1], "share": share.get(k, 0.0)}
-                    for k, v in kern.items() if v[1] > 0},
+        "roofline": roof,
+        "kernels": head["kernels"],
         "profiled_ms_per_step": ms_profiled / args.steps,
         "gpu_launches": int(launches),
+        other: sub,
         "clocks": clk.summary(),
         "status": int(status),
     }
+    if main == "fused":
+        line["step_frac_5pass_320"] = head["step_frac_5pass_320"]
     ctx.close()
+    del hu, hb
+    if not args.no_512 and world == 1:
+        # the 256^3 launch shapes do not carry over: the 512^3 leg runs the planner's own choices
+        from heterogeneous_mhd_gb300 import autotune
+        autotune.apply({})
+        line["size512"] = size512_leg(mhd, torch)
+        autotune.apply(tuned)
     if not args.no_fp64:
         line["fp64_error"] = fp64_error_leg(mhd, n, args.fp64_steps)
     if not args.no_batch:
@@ -453,6 +529,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-boxes leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error leg")
     ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure leg")
+    ap.add_argument("--no-512", action="store_true", help="skip the 512^3 plain-step leg")
     ap.add_argument("--ncu-case", action="store_true", help="run the short profiling case only")
     ap.add_argument("--knob", action="append", default=[], help="launch-shape knob key=value for --ncu-case")
     ap.add_argument("--fp64-steps", type=int, default=100, help="steps of the FP64 error leg")

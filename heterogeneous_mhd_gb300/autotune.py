@@ -22,7 +22,7 @@ from . import Context, init_turbulence, lib
 
 CACHE = Path(os.environ.get("MHD_GB300_TUNE_CACHE", Path(__file__).resolve().parent / "lib" / "tuning.json"))
 KNOBS = ("fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K", "fluidx.cells", "advect.kernel",
-         "advect.xk")
+         "advect.xk", "sweep.kernel", "sweep.k", "sweep.slots")
 
 
 def set_knob(key: str, value: int) -> None:

@@ -8,8 +8,10 @@
 #include "mhd_advect2.cuh"
 #include "mhd_advect3.cuh"
 #include "mhd_advect4.cuh"
+#include "mhd_advect5.cuh"
 #include "mhd_fluidx2.cuh"
 #include "mhd_launch.h"
+#include "mhd_tmap.h"
 #include "mhd_transpose2.cuh"
 #include "mhd_transpose3.cuh"
 
@@ -87,33 +89,46 @@ template <int C, int T, int AX = 0>
 static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
 {
     static bool attr = false;
-    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T, AX>, attr, AX == 0);
+    cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T, AX>, attr, true);
     if (e != cudaSuccess)
         return e;
     // grid: (pencil groups along j, planes along k, boxes)
     const int nj = (AX == 0) ? a.ny : a.nx, nk = (AX == 2) ? a.ny : a.nz;
     dim3 grid(nj / a.P, nk, a.bs.count);
-    k_fluidx2<R, EX, C, T, AX><<<grid, a.P * T, fluidx2_smem_elems(C * T, a.P, AX) * sizeof(R), s>>>(a);
+    SweepMaps tm{};
+    size_t smem = fluidx2_smem_elems(C * T, a.P) * sizeof(R);
+    if constexpr (AX != 0) {
+        // the x-major state as (5 nx words, ny, nz) for u and (3 nx, ny, nz) for b;
+        // boxes of P cells along x by the whole pencil along y (AX 1) or z (AX 2)
+        constexpr int n = C * T;
+        const uint32_t by = (AX == 1) ? n : 1, bz = (AX == 1) ? 1 : n;
+        const uint64_t ny = a.ny, nz = a.nz;
+        e = encode_map_3d(&tm.u_in, a.uu, 5ull * a.nx, ny, nz, 5 * kSweepP, by, bz);
+        if (e == cudaSuccess)
+            e = encode_map_3d(&tm.b_in, a.ub, 3ull * a.nx, ny, nz, 3 * kSweepP, by, bz);
+        if (e == cudaSuccess)
+            e = encode_map_3d(&tm.bn_in, a.ub, 3ull * a.nx, ny, nz, 4, by, bz);
+        if (e == cudaSuccess)
+            e = encode_map_3d(&tm.u_out, a.u_out, 5ull * a.nx, ny, nz, 5 * kSweepP, by, bz);
+        if (e != cudaSuccess)
+            return e;
+        smem = fluidx_sweep_smem_bytes(n);
+    }
+    k_fluidx2<R, EX, C, T, AX><<<grid, a.P * T, smem, s>>>(a, tm);
     return cudaGetLastError();
 }
 
-// Sweep of the untransposed state along y or z (fused step): the pencil
-// length is ny or nz, P pencils at consecutive x per CTA.
-static bool plan_fluidx_sweep(int n, int nx, FxPlan& p)
+// Sweep of the untransposed state along y or z (fused step, FP32): pencils
+// of n = 4T <= 256 cells along the sweep (one tensor box), four pencils at
+// consecutive x per CTA (nx a multiple of 4, so every box starts on a
+// 16-byte boundary), one box of the state.
+static bool plan_fluidx_sweep(int n, int nx, int nbox, FxPlan& p)
 {
     p = FxPlan{0, 0, 0};
-    if (!kV2)
+    if (!kV2 || nbox != 1 || n % 4 != 0 || !pow2_in(n / 4, 8, 64) || nx % kSweepP != 0)
         return false;
-    if (n % 4 == 0 && pow2_in(n / 4, 8, 128))
-        p.C = 4, p.T = n / 4;
-    else if (n % 3 == 0 && n % 4 == 0 && pow2_in(n / 3, 16, 128))
-        p.C = 3, p.T = n / 3;
-    else
-        return false;
-    for (int P = 1; P <= 8 && P <= nx; P++)
-        if (nx % P == 0 && P * p.T <= 256 && (P * p.T) % 32 == 0)
-            p.P = P;
-    return p.P > 0;
+    p.C = 4, p.T = n / 4, p.P = kSweepP;
+    return true;
 }
 
 template <int AX>
@@ -121,21 +136,11 @@ static cudaError_t fluidx_sweep(FluidxArgs a, const FxPlan& p, cudaStream_t s)
 {
     if constexpr (kV2) {
         a.P = p.P;
-        if (p.C == 4) {
-            switch (p.T) {
-            case 8: return launch_fx2<4, 8, AX>(a, s);
-            case 16: return launch_fx2<4, 16, AX>(a, s);
-            case 32: return launch_fx2<4, 32, AX>(a, s);
-            case 64: return launch_fx2<4, 64, AX>(a, s);
-            case 128: return launch_fx2<4, 128, AX>(a, s);
-            }
-        } else {
-            switch (p.T) {
-            case 16: return launch_fx2<3, 16, AX>(a, s);
-            case 32: return launch_fx2<3, 32, AX>(a, s);
-            case 64: return launch_fx2<3, 64, AX>(a, s);
-            case 128: return launch_fx2<3, 128, AX>(a, s);
-            }
+        switch (p.T) {
+        case 8: return launch_fx2<4, 8, AX>(a, s);
+        case 16: return launch_fx2<4, 16, AX>(a, s);
+        case 32: return launch_fx2<4, 32, AX>(a, s);
+        case 64: return launch_fx2<4, 64, AX>(a, s);
         }
     }
     return cudaErrorInvalidValue;
@@ -146,7 +151,10 @@ static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
     FluidxArgs a = in;
     if (a.axis != 0) {
         FxPlan p;
-        if (a.cfl_part || !plan_fluidx_sweep(a.axis == 1 ? a.ny : a.nz, a.nx, p))
+        const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.uu) |
+                             reinterpret_cast<uintptr_t>(a.ub);
+        if (a.cfl_part || a.w_out || (al & 15) != 0 ||
+            !plan_fluidx_sweep(a.axis == 1 ? a.ny : a.nz, a.nx, a.bs.count, p))
             return cudaErrorInvalidValue;
         return (a.axis == 1) ? fluidx_sweep<1>(a, p, s) : fluidx_sweep<2>(a, p, s);
     }
@@ -394,6 +402,79 @@ static cudaError_t advect_x4(const AdvectArgs& a, const A4Plan& p, cudaStream_t 
     return cudaErrorInvalidValue;
 }
 
+// Sweep-walking kernel of the fused step's sweeps along y and z (FP32, one
+// box): lanes along x (nx a multiple of 32), KT planes per CTA (4 by default,
+// or sweep.k), NS chunk buffers (3, or 2 by sweep.slots), the pencil length a
+// multiple of 4.  sweep.kernel = 3 keeps the marching kernel instead.
+static bool plan_advect5(const AdvectArgs& a, A4Plan& p)
+{
+    if (!kV2 || a.axis == 0 || a.b1_src != a.ub || a.bs.count != 1 || tune_value(TUNE_SWEEP_KERNEL) == 3)
+        return false;
+    const int n = (a.axis == 1) ? a.ny : a.nz, nk = (a.axis == 1) ? a.nz : a.ny;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.uu) |
+                         reinterpret_cast<uintptr_t>(a.ub);
+    if ((al & 15) != 0 || a.nx % kA5J != 0 || n % kA4X != 0)
+        return false;
+    const int kt = tune_value(TUNE_SWEEP_K);
+    p.NS = (tune_value(TUNE_SWEEP_SLOTS) == 2) ? 2 : 3;
+    p.KT = 0;
+    for (int k : {4, 8, 2})
+        if (!p.KT && (kt == 0 || kt == k) && nk % k == 0)
+            p.KT = k;
+    return p.KT != 0;
+}
+
+template <int KT, int NS, int AX>
+static cudaError_t launch_ad5(const AdvectArgs& a, cudaStream_t s)
+{
+    static bool attr = false;
+    static int per_sm_of[kMaxOccDevices] = {}, nsm_of[kMaxOccDevices] = {};
+    cudaError_t e = allow_smem(k_advect5<EX, KT, NS, AX>, attr, true);
+    if (e != cudaSuccess)
+        return e;
+    const size_t smem = advect5_smem_bytes(KT, NS);
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= kMaxOccDevices)
+        return cudaErrorInvalidDevice;
+    int& per_sm = per_sm_of[dev];
+    int& nsm = nsm_of[dev];
+    if (!per_sm) {
+        e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect5<EX, KT, NS, AX>, advect5_threads(KT),
+                                                              smem);
+        if (e != cudaSuccess)
+            return e;
+        if (per_sm < 1)
+            return cudaErrorInvalidConfiguration;
+    }
+    const int n = (AX == 1) ? a.ny : a.nz, nk = (AX == 1) ? a.nz : a.ny;
+    const long long work = (long long)(a.nx / kA5J) * (nk / KT) * (n / kA4X);
+    long long ctas = (long long)per_sm * nsm;
+    const long long cap = (work / 8 > 0) ? work / 8 : 1;
+    if (ctas > cap)
+        ctas = cap;
+    k_advect5<EX, KT, NS, AX><<<dim3((unsigned)ctas, 1, 1), advect5_threads(KT), smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int AX>
+static cudaError_t advect_y5(const AdvectArgs& a, const A4Plan& p, cudaStream_t s)
+{
+    switch (p.KT * 10 + p.NS) {
+    case 82: return launch_ad5<8, 2, AX>(a, s);
+    case 83: return launch_ad5<8, 3, AX>(a, s);
+    case 42: return launch_ad5<4, 2, AX>(a, s);
+    case 43: return launch_ad5<4, 3, AX>(a, s);
+    case 22: return launch_ad5<2, 2, AX>(a, s);
+    case 23: return launch_ad5<2, 3, AX>(a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
 template <int C, int T>
 static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
 {
@@ -410,6 +491,11 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
 {
     AdvectArgs a = in;
     if (a.axis != 0) {  // fused step: pencils along y or z of the untransposed state
+        if constexpr (kV2) {
+            A4Plan p5;
+            if (plan_advect5(a, p5))
+                return (a.axis == 1) ? advect_y5<1>(a, p5, s) : advect_y5<2>(a, p5, s);
+        }
         A3Plan p3;
         const int n = (a.axis == 1) ? a.ny : a.nz, nk = (a.axis == 1) ? a.nz : a.ny;
         if (!kV2 || a.b1_src != a.ub || !plan_advect3(n, a.nx, nk, true, p3, a.axis))
@@ -546,13 +632,19 @@ static cudaError_t divb(const void* b, int nx, int ny, int nz, double* part, int
     return cudaGetLastError();
 }
 
-// the fused step's sweeps along y and z have kernels for this shape
+// the fused step's sweeps along y and z have kernels for this shape (one box)
 static int fused_ok(int nx, int ny, int nz)
 {
     FxPlan p;
     A3Plan q;
-    return plan_fluidx_sweep(ny, nx, p) && plan_fluidx_sweep(nz, nx, p) && plan_advect3(ny, nx, nz, true, q, 1) &&
-           plan_advect3(nz, nx, ny, true, q, 2);
+    A4Plan q5;
+    auto advect_ok = [&](int axis) {
+        AdvectArgs a{};
+        a.nx = nx, a.ny = ny, a.nz = nz, a.axis = axis, a.bs.count = 1;
+        const int n = (axis == 1) ? ny : nz, nk = (axis == 1) ? nz : ny;
+        return plan_advect5(a, q5) || plan_advect3(n, nx, nk, true, q, axis);
+    };
+    return plan_fluidx_sweep(ny, nx, 1, p) && plan_fluidx_sweep(nz, nx, 1, p) && advect_ok(1) && advect_ok(2);
 }
 
 // nonzero if the x-sweep fluidx of this grid is k_fluidx2 (which writes the

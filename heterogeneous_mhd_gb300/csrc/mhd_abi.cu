@@ -925,7 +925,8 @@ long long mhd::tune_generation() { return g_tune_gen.load(); }
 static int tune_key(const char* key)
 {
     static const char* names[TUNE_COUNT] = {"fluidx.threads", "advect.cells", "advect.slots", "advect.J", "advect.K",
-                                            "fluidx.cells", "advect.kernel", "advect.xk"};
+                                            "fluidx.cells", "advect.kernel", "advect.xk", "sweep.kernel",
+                                            "sweep.k", "sweep.slots"};
     if (!key)
         return -1;
     for (int k = 0; k < TUNE_COUNT; k++)

@@ -8,13 +8,19 @@
 //
 // AX = 1, 2: the same sweep along y or z of the untransposed state (the fused
 // step's replacement for transpose12/13 + fluidx + transpose back).  The CTA
-// owns P pencils at consecutive x; the rows (the P cells at one position
-// along the sweep, contiguous in x) are read word by word by consecutive
-// threads into the pencil-major shared layout the engine reads (pencil stride
-// padded by kSweepPad), the components seen in the order the transposed call
-// would see them (C/transpose12.c:7-47, C/transpose13.c:9-62), and the new
-// rows go back the same way.  The arithmetic is the x sweep's.
+// owns P = 4 pencils at consecutive x.  Its rows (the P cells at one position
+// along the sweep, contiguous in x) arrive by 3-D tensor copies
+// (cp.async.bulk.tensor, one per array: u, b, b of plane k+1 and b of the
+// pencil after the group), then one pass over shared memory, with a
+// bank-conflict-free thread mapping, builds the cell-centred field and a
+// second one turns the u rows into the pencil-major layout the engine reads;
+// the new pencils go back the same way and leave by one tensor store.  The
+// components are seen in the order the transposed call would see them
+// (C/transpose12.c:7-47, C/transpose13.c:9-62); the arithmetic is the x
+// sweep's.
 #pragma once
+#include <cuda.h>  // CUtensorMap
+
 #include "mhd_kernels.cuh"
 #include "mhd_pencil.cuh"
 
@@ -25,17 +31,49 @@ struct Fx2Shape {
     static constexpr int N = C * T;  // cells per pencil
 };
 
-// shared memory (elements of R): su P pencils of 5n, sb P+1 pencils of 3n, sbk P of 3n, red 32,
-// seam 2*32*10; the y/z sweeps pad each pencil by kSweepPad
-__host__ __device__ inline size_t fluidx2_smem_elems(int n, int P, int ax = 0)
+// shared memory (elements of R) of the x sweep: su P pencils of 5n, sb P+1
+// pencils of 3n, sbk P of 3n, red 32, seam 2*32*10
+__host__ __device__ inline size_t fluidx2_smem_elems(int n, int P)
 {
-    const size_t su = 5 * (size_t)n + (ax ? kSweepPad : 0), sb = 3 * (size_t)n + (ax ? kSweepPad : 0);
-    return P * su + (P + 1) * sb + P * sb + 32 + 2 * 32 * 10;
+    return P * 5 * (size_t)n + (P + 1) * 3 * (size_t)n + P * 3 * (size_t)n + 32 + 2 * 32 * 10;
+}
+
+// Tensor maps of one sweep along y or z, encoded by the launcher: u and b of
+// the input state with boxes of P cells along x by the whole pencil, b with a
+// box of four words (the b of cell x0+P and one word after it) for the pencil
+// after the group, and u of the output state.
+struct SweepMaps {
+    CUtensorMap u_in, b_in, bn_in, u_out;
+};
+
+// Sweeps along y and z: P = 4 pencils of n = 4T cells per CTA, n <= 256 (one
+// tensor box per array).  Pencil strides of the pencil-major u and field are
+// 8 words more than 5n and 3n (both n % 32 == 0 or 8-word aligned), which
+// keeps the transposing passes free of bank conflicts.
+constexpr int kSweepP = 4;
+__host__ __device__ constexpr int sweep_su(int n) { return 5 * n + 8; }
+__host__ __device__ constexpr int sweep_sf(int n) { return 3 * n + 8; }
+
+// Shared memory of a sweep along y or z (bytes): staged u rows [n][5P];
+// region B: staged b rows [n][3P], b rows of plane k+1 [n][3P] and b rows of
+// the next pencil [n][4], which the pencil-major u [P][SU] replaces once the
+// field is built; the cell-centred field [P][SF]; red and seam; 128 bytes of
+// alignment slack (the tensor copies want 128-byte aligned buffers).
+__host__ __device__ inline size_t fluidx_sweep_regb(int n)
+{
+    const size_t st = (size_t)n * (6 * kSweepP + 4), su = (size_t)kSweepP * sweep_su(n);
+    return st > su ? st : su;
+}
+__host__ __device__ inline size_t fluidx_sweep_smem_bytes(int n)
+{
+    return ((size_t)n * 5 * kSweepP + fluidx_sweep_regb(n) + (size_t)kSweepP * sweep_sf(n) + 32 + 2 * 32 * 10) *
+               sizeof(float) + 128;
 }
 
 template <typename R, bool EX, int C, int T, int AX = 0>
-__global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
+__global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const __grid_constant__ SweepMaps tm)
 {
+    static_assert(AX == 0 || (sizeof(R) == 4 && C == 4 && T <= 64), "sweeps along y, z: FP32, 4 cells, n <= 256");
     select_box(a, blockIdx.z, sizeof(CflPart<R>));
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -49,12 +87,18 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
     const int kp = (k + 1 == a.nz) ? 0 : k + 1;
     const int jn = (j0 + P == a.ny) ? 0 : j0 + P;
 
-    constexpr int SU = 5 * n + (AX ? kSweepPad : 0), SB = 3 * n + (AX ? kSweepPad : 0);  // pencil strides
-    R* su = reinterpret_cast<R*>(smem_raw);
-    R* sb = su + P * SU;
-    R* sbk = sb + (P + 1) * SB;
-    R* red = sbk + P * SB;
-    R* seam = red + 32;
+    // pencil strides; x sweep: su [P][5n], sb [P+1][3n], sbk [P][3n]; y/z
+    // sweeps: the staged rows, su [P][SU] over the staged b, the field sf [P][SF]
+    constexpr int SU = AX ? sweep_su(n) : 5 * n, SB = AX ? sweep_sf(n) : 3 * n;
+    R* const base = AX ? reinterpret_cast<R*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127))
+                       : reinterpret_cast<R*>(smem_raw);
+    R* const rows_u = base;                                       // y/z: [n][5P]
+    R* const su = AX ? base + n * 5 * kSweepP : base;
+    R* const sb = AX ? nullptr : su + P * SU;
+    R* const sbk = AX ? nullptr : sb + (P + 1) * SB;
+    R* const sf = AX ? su + fluidx_sweep_regb(n) : nullptr;      // y/z: [P][SF]
+    R* const red = AX ? sf + P * SB : sbk + P * SB;
+    R* const seam = red + 32;
     __shared__ uint64_t bar;
 
     const R* uu = static_cast<const R*>(a.uu);
@@ -79,28 +123,62 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
         if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
             return;
     } else {
-        // rows of P cells (x0..x0+P-1) at plane k and k+1, and the b of x0+P;
-        // consecutive threads read consecutive words of a row
+        // the rows of the group (x0..x0+P-1) along the whole pencil at plane kk,
+        // its b rows at plane kn, and the b of cell x0+P (periodic)
         const int x0 = blockIdx.x * P, kk = blockIdx.y;
         const int nk = (AX == 1) ? a.nz : a.ny;
         const int kn = (kk + 1 == nk) ? 0 : kk + 1;
         const int xn = (x0 + P == a.nx) ? 0 : x0 + P;
-        const int nt = blockDim.x;
-        // rows along the sweep are rstride cells apart; 4-byte cp.async, all in flight at once
-        const size_t rs = (AX == 1) ? (size_t)a.nx : (size_t)a.nx * a.ny;
-        if constexpr (sizeof(R) == 4) {
-            const float* u0 = reinterpret_cast<const float*>(uu) + sweep_cell<AX>(0, x0, kk, a.nx, a.ny) * 5;
-            const float* b0 = reinterpret_cast<const float*>(ub) + sweep_cell<AX>(0, x0, kk, a.nx, a.ny) * 3;
-            const float* bk0 = reinterpret_cast<const float*>(ub) + sweep_cell<AX>(0, x0, kn, a.nx, a.ny) * 3;
-            const float* bn0 = reinterpret_cast<const float*>(ub) + sweep_cell<AX>(0, xn, kk, a.nx, a.ny) * 3;
-            auto same = [](int p) { return p; };
-            auto zero = [](int) { return 0; };
-            gather_tile<5>(reinterpret_cast<float*>(su), SU, u0, rs * 5, P, n, same, tid, nt);
-            gather_tile<3>(reinterpret_cast<float*>(sb), SB, b0, rs * 3, P, n, same, tid, nt);
-            gather_tile<3>(reinterpret_cast<float*>(sbk), SB, bk0, rs * 3, P, n, same, tid, nt);
-            gather_tile<3>(reinterpret_cast<float*>(sb) + P * SB, SB, bn0, rs * 3, 1, n, zero, tid, nt);
-            cp_async_commit();
-            cp_async_wait<0>();
+        R* const rows_b = su;                          // [n][3P]
+        R* const rows_bk = rows_b + n * 3 * kSweepP;   // [n][3P]
+        R* const rows_bn = rows_bk + n * 3 * kSweepP;  // [n][4]
+        if (tid == 0) {
+            mbar_init(&bar, 1);
+            mbar_arrive_expect_tx(&bar, (uint32_t)(n * (5 * kSweepP + 6 * kSweepP + 4) * sizeof(R)));
+            // coordinates (x word, y, z): the pencil runs along y (AX 1) or z (AX 2) from 0
+            const int y = (AX == 1) ? 0 : kk, z = (AX == 1) ? kk : 0;
+            const int yk = (AX == 1) ? 0 : kn, zk = (AX == 1) ? kn : 0;
+            tma_load_3d(rows_u, &tm.u_in, 5 * x0, y, z, &bar);
+            tma_load_3d(rows_b, &tm.b_in, 3 * x0, y, z, &bar);
+            tma_load_3d(rows_bk, &tm.b_in, 3 * x0, yk, zk, &bar);
+            tma_load_3d(rows_bn, &tm.bn_in, 3 * xn, y, z, &bar);
+        }
+        __syncthreads();
+        if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
+            return;  // a copy never landed (error bit set)
+        // cell-centred field (C/fluidx.c:71-81) of cell (r, p), seen in the
+        // transposed order: b_d averaged with the next row, b_x with the next
+        // pencil, b_k with the next plane.  Thread e takes cell (e / P, e % P):
+        // the staged rows are read at a stride of three words, sf is written
+        // with a pencil stride of 8 (mod 32) words, both without bank conflicts.
+        constexpr int B0 = sweep_b<AX>(0), B1 = sweep_b<AX>(1), B2 = sweep_b<AX>(2);
+        for (int e = tid; e < n * kSweepP; e += blockDim.x) {
+            const int r = e / kSweepP, p = e - r * kSweepP;
+            const int rn = (r + 1 == n) ? 0 : r + 1;
+            const R* bc = rows_b + r * 3 * kSweepP + 3 * p;
+            const R bd = bc[B0], bdn = rows_b[rn * 3 * kSweepP + 3 * p + B0];
+            const R bj = bc[B1], bjn = (p + 1 < kSweepP) ? bc[3 + B1] : rows_bn[r * 4 + B1];
+            const R bk = bc[B2], bkn = rows_bk[r * 3 * kSweepP + 3 * p + B2];
+            R* o = sf + p * SB + 3 * r;
+            if constexpr (EX) {
+                o[0] = R(0.5) * bd + R(0.5) * bdn;
+                o[1] = R(0.5) * bj + bjn / R(2);
+                o[2] = R(0.5) * bk + bkn / R(2);
+            } else {  // the same values: halving is exact
+                o[0] = R(0.5) * (bd + bdn);
+                o[1] = R(0.5) * (bj + bjn);
+                o[2] = R(0.5) * (bk + bkn);
+            }
+        }
+        __syncthreads();  // the staged b is dead: su takes its place
+        // u rows -> pencil-major, raw component order (stride-5 reads, 8 (mod 32) pencil stride)
+        for (int e = tid; e < n * kSweepP; e += blockDim.x) {
+            const int r = e / kSweepP, p = e - r * kSweepP;
+            const R* src = rows_u + 5 * e;
+            R* dst = su + p * SU + 5 * r;
+#pragma unroll
+            for (int c = 0; c < 5; c++)
+                dst[c] = src[c];
         }
         __syncthreads();
     }
@@ -122,6 +200,16 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
                 q[m][s] = qf[5 * m + sweep_u<AX>(s)];
     };
     auto load_f = [&](R (&f)[C][3]) {  // C/fluidx.c:71-81: b/2 + b(neighbour face)/2
+        if constexpr (AX != 0) {  // built once from the staged rows
+            R ff[C * 3];
+            lds_chunk<R, C * 3>(sf + (size_t)lp * SB + (size_t)i0 * 3, ff);
+#pragma unroll
+            for (int m = 0; m < C; m++)
+#pragma unroll
+                for (int s = 0; s < 3; s++)
+                    f[m][s] = ff[3 * m + s];
+            return;
+        }
         R bjf[C * 3], bpf[C * 3], bkf[C * 3];
         const R* bj = sb + (size_t)lp * SB;
         lds_chunk<R, C * 3>(bj + 3 * i0, bjf);
@@ -369,12 +457,23 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a)
             tma_store_wait_all();
         }
     } else {
+        // pencil-major -> rows (the mapping of the gather, reversed), then one tensor store
         __syncthreads();
-        if constexpr (sizeof(R) == 4) {
+        for (int e = tid; e < n * kSweepP; e += blockDim.x) {
+            const int r = e / kSweepP, p = e - r * kSweepP;
+            const R* src = su + p * SU + 5 * r;
+            R* dst = rows_u + 5 * e;
+#pragma unroll
+            for (int c = 0; c < 5; c++)
+                dst[c] = src[c];
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
             const int x0 = blockIdx.x * P, kk = blockIdx.y;
-            const size_t rs = (AX == 1) ? (size_t)a.nx : (size_t)a.nx * a.ny;
-            float* uo = static_cast<float*>(a.u_out) + sweep_cell<AX>(0, x0, kk, a.nx, a.ny) * 5;
-            scatter_tile<5>(uo, rs * 5, reinterpret_cast<const float*>(su), SU, P, n, tid, blockDim.x);
+            tma_store_3d(&tm.u_out, 5 * x0, (AX == 1) ? 0 : kk, (AX == 1) ? kk : 0, rows_u);
+            tma_store_commit();
+            tma_store_wait_all();
         }
     }
 }

@@ -56,6 +56,9 @@ enum TuneKey : int {
     TUNE_FLUIDX_C,            // cells per thread of the register-resident fluidx (4, or 8: one warp per pencil)
     TUNE_ADVECT_KERNEL,       // advectbyzx of the x sweep: 3 marching along k, 4 walking along x
     TUNE_ADVECT_XK,           // planes per CTA of the x-walking advectbyzx (2, 4 or 8)
+    TUNE_SWEEP_KERNEL,        // advectbyzx of the fused step's y/z sweeps: 5 walking (default), 3 marching
+    TUNE_SWEEP_K,             // planes per CTA of the sweep-walking advectbyzx (2, 4 or 8)
+    TUNE_SWEEP_SLOTS,         // chunk buffers of the sweep-walking advectbyzx (2 or 3)
     TUNE_COUNT
 };
 int tune_value(int key);

@@ -104,6 +104,29 @@ __device__ __forceinline__ void fence_proxy_async_smem()
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Tiled 3-D tensor copies (cp.async.bulk.tensor) through a tensor map that
+// lives in kernel parameter space (a __grid_constant__ argument); coordinates
+// are in elements, innermost first.  The load completes on an mbarrier, the
+// store joins the issuing thread's bulk group.  The shared buffer is 128-byte
+// aligned and the innermost coordinate times the element size a multiple of
+// 16 bytes (checked by the callers' planners).
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int c0, int c1, int c2, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_3d(const void* tmap, int c0, int c1, int c2, const void* src)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     reinterpret_cast<uint64_t>(tmap)),
+                 "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
+                 : "memory");
+}
+
 // 4-byte asynchronous global -> shared copy (per thread; completion through
 // cp.async groups), used where a tile must be scattered element by element.
 __device__ __forceinline__ void cp_async4(void* dst, const void* src)

@@ -173,8 +173,11 @@ MHD_API long long mhd_launch_count(mhd_ctx *ctx);
  * (plane-slab ring depth: 2 or 3; chunk buffers of the x-walking kernel),
  * "advect.J" (pencils per CTA), "advect.K" (planes per CTA), "fluidx.cells"
  * (4, or 8: one warp per pencil), "advect.kernel" (3: the marching
- * advectbyzx, 4: the x-walking one) and "advect.xk" (planes per CTA of the
- * x-walking kernel: 2, 4 or 8).  0 restores the planner's own choice; a value that does
+ * advectbyzx, 4: the x-walking one), "advect.xk" (planes per CTA of the
+ * x-walking kernel: 2, 4 or 8), and for the fused step's sweeps along y and z
+ * "sweep.kernel" (5: the sweep-walking advectbyzx, 3: the marching one),
+ * "sweep.k" (its planes per CTA: 2, 4 or 8) and "sweep.slots" (its chunk
+ * buffers: 2 or 3).  0 restores the planner's own choice; a value that does
  * not fit the grid is ignored.  Captured step graphs are rebuilt on the next
  * mhd_step.  mhd_tune_get returns the current value (-1 for an unknown key). */
 MHD_API int mhd_tune_set(const char *key, int value);

@@ -73,3 +73,25 @@ def test_fused_non_cubic_runs_where_plain_cannot(mhd, cuda):
         u, b = ctx.get_state()
         assert np.all(np.isfinite(u)) and np.all(np.isfinite(b))
         assert ctx.divb_max() <= 2e-6 * float(np.abs(b).max())
+
+
+@pytest.mark.parametrize("knobs", [{}, {"sweep.k": 2}, {"sweep.k": 8}, {"sweep.slots": 2},
+                                   {"sweep.k": 2, "sweep.slots": 2}, {"sweep.kernel": 3}])
+@pytest.mark.parametrize("shape", [(32, 64, 64), (128, 32, 32), (64, 128, 128)])
+def test_fused_sweep_kernels_exact_vs_oracle(shape, knobs, mhd, cuda, oracle32):
+    """Every launch shape of the sweep kernels along y and z (the walking
+    advectbyzx with 2, 4 or 8 planes per CTA and 2 or 3 chunk buffers, and the
+    marching one by sweep.kernel = 3; fluidx with its tensor-copied tiles) on
+    boxes whose three axes have different lengths: EXACT fused steps bit for
+    bit against the oracle of the reference's C path.  The x sweeps keep
+    their own kernels."""
+    from heterogeneous_mhd_gb300 import autotune
+    u0, b0 = mhd.init_vortex(*shape, seed=4, vscale=1.3)
+    ref = oracle32.strang(u0, b0, *shape, 2)
+    try:
+        autotune.apply(knobs)
+        u, b, t = run(mhd, u0, b0, shape, 2, fused=True, exact=True)
+    finally:
+        autotune.apply({k: 0 for k in knobs})
+    assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1]), (shape, knobs)
+    assert np.float32(t) == np.float32(ref[2])
