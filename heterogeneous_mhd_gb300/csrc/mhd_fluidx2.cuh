@@ -90,8 +90,10 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const
     // pencil strides; x sweep: su [P][5n], sb [P+1][3n], sbk [P][3n]; y/z
     // sweeps: the staged rows, su [P][SU] over the staged b, the field sf [P][SF]
     constexpr int SU = AX ? sweep_su(n) : 5 * n, SB = AX ? sweep_sf(n) : 3 * n;
-    R* const base = AX ? reinterpret_cast<R*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127))
-                       : reinterpret_cast<R*>(smem_raw);
+    // the 128-byte aligned start is an offset from smem_raw (not a pointer rebuilt
+    // from an integer), so every access below stays a shared-memory access
+    const uint32_t pad = (128u - (static_cast<uint32_t>(__cvta_generic_to_shared(smem_raw)) & 127u)) & 127u;
+    R* const base = reinterpret_cast<R*>(smem_raw + (AX ? pad : 0u));
     R* const rows_u = base;                                       // y/z: [n][5P]
     R* const su = AX ? base + n * 5 * kSweepP : base;
     R* const sb = AX ? nullptr : su + P * SU;
