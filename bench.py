@@ -173,11 +173,44 @@ def cpu_baseline(size: int, seconds: float = 12.0):
             break
     single = 64 ** 3 * steps1 / (time.perf_counter() - t1)
     port.set_threads(cores)
-    return {"value": size ** 3 * steps / el, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+    out = {"value": size ** 3 * steps / el, "unit": "cell-updates/s", "cores": cores, "kind": "port",
             "sample": f"{steps} full Strang steps of the {size}^3 turbulence box, oracle restatement of the "
                       f"reference C path with OpenMP over pencils ({cores} threads)",
             "single_core": {"value": single, "unit": "cell-updates/s", "cores": 1,
                             "sample": f"{steps1} Strang steps of the 64^3 vortex on one thread"}}
+    rb = reference_build_timing()
+    if rb:
+        out["reference_build"] = rb
+    return out
+
+
+def reference_build_timing(o2_size: int = 128, o0_size: int = 64):
+    """The reference's own C/ operators (oracle/_ref, compiled from its
+    sources on this host), single-threaded as written, driven by the loop of
+    C/mhd.c:59-124 with its copy_matrix calls: one Strang step of the
+    turbulence box at o2_size^3 with -O2, and at o0_size^3 built as
+    C/makefile builds it (no optimisation flags).  None when this host has no
+    build of the reference."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _oracle import REF, REF_O0, Oracle
+
+    if not REF[32].exists():
+        return None
+    port = Oracle(32, "port")
+    out = {}
+    for key, kind, n, path in (("O2", "ref", o2_size, REF[32]), ("O0", "ref_O0", o0_size, REF_O0)):
+        if not path.exists():
+            continue
+        ref = Oracle(32, kind)
+        u, b = port.init_turbulence(n, seed=0)
+        t0 = time.perf_counter()
+        ref.strang(u, b, n, n, n, 1)
+        el = time.perf_counter() - t0
+        out[key] = {"value": n ** 3 / el, "unit": "cell-updates/s", "cores": 1, "kind": "reference",
+                    "sample": f"one Strang step of the {n}^3 turbulence box, the reference's C/ operators built "
+                              f"with {'-O2' if key == 'O2' else 'no optimisation flags (as C/makefile)'}, "
+                              f"one thread, {el:.2f} s"}
+    return out
 
 
 def reference_arm(args):
@@ -208,6 +241,9 @@ def reference_arm(args):
                                        f"oracle/mhd_oracle.c (bit-identical to the reference build), OpenMP over "
                                        f"pencils, {cores} threads"},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    rb = reference_build_timing()
+    if rb:
+        line["cpu_baseline"]["reference_build"] = rb
     print(json.dumps(line), flush=True)
 
 

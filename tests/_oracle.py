@@ -20,6 +20,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[1]
 PORT = {32: ROOT / "oracle" / "_build" / "liboracle_f32.so", 64: ROOT / "oracle" / "_build" / "liboracle_f64.so"}
 REF = {32: ROOT / "oracle" / "_ref" / "libmhdref_f32.so", 64: ROOT / "oracle" / "_ref" / "libmhdref_f64.so"}
+# the reference's C/ built without optimisation, as its own makefile does (timing only)
+REF_O0 = ROOT / "oracle" / "_ref" / "libmhdref_f32_O0.so"
 
 
 def build() -> None:
@@ -28,7 +30,7 @@ def build() -> None:
 
 class Oracle:
     def __init__(self, bits: int = 32, kind: str = "port"):
-        path = (PORT if kind == "port" else REF)[bits]
+        path = REF_O0 if kind == "ref_O0" else (PORT if kind == "port" else REF)[bits]
         if not path.exists():
             build()
         if not path.exists():
