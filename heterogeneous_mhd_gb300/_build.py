@@ -97,24 +97,5 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return lib
 
 
-# where `make -C oracle ship` leaves the reference's operator sources (git-ignored)
-SHIPPED_REF = ROOT / "baseline" / "_ref" / "C"
-
-
-def build_oracle(ship: bool = False) -> None:
-    """Build the CPU oracle (test infrastructure) with its own Makefile.
-
-    The reference's own C/ build (oracle/_ref) is made from MHD_REF_SRC when
-    set, else from the copy shipped in baseline/_ref/C when present.  With
-    `ship`, MHD_REF_SRC's files are first copied there so that they travel
-    with the working tree."""
-    if not os.environ.get("MHD_REF_SRC") and SHIPPED_REF.is_dir():
-        os.environ["MHD_REF_SRC"] = str(SHIPPED_REF)
-    if ship and os.environ.get("MHD_REF_SRC") and Path(os.environ["MHD_REF_SRC"]).resolve() != SHIPPED_REF.resolve():
-        _run(["make", "-s", "-C", str(ROOT / "oracle"), "ship"])
-    _run(["make", "-s", "-C", str(ROOT / "oracle"), "all"])
-
-
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
-    build_oracle()
