@@ -365,10 +365,12 @@ def _run_to(ctx: Context, tf: float, cfl: float, chunk: int, corrector=None, str
 
 
 def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossings=(0.5, 1.0, 2.0),
-             cfl: float = 0.7, log=_log, gain: float = 1.0) -> dict:
+             cfl: float = 0.7, log=_log, gain: float = 1.0, gains=None) -> dict:
     """Held-out seeds run to each horizon (in turbulent crossing times L / v_rms)
     three ways; errors against the filtered fine run at every horizon, GPU
-    time to the last one."""
+    time to the last one.  With `gains`, the corrected coarse run is repeated
+    for every gain (the fine run once per seed); "closure" is the first."""
+    gains = [float(g) for g in (gains if gains else [gain])]
     torch = _torch()
     horizons = sorted(float(c) for c in (crossings if np.iterable(crossings) else [crossings]))
     nc = fine // factor
@@ -406,11 +408,12 @@ def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossi
         _check(L.mhd_cl_filter(du.data_ptr(), db.data_ptr(), fine, factor, uci.data_ptr(), bci.data_ptr(),
                                cl.stream_ptr()), "filter")
         torch.cuda.synchronize()
-        for label, use in (("plain", False), ("closure", True)):
+        for label, g in [("plain", None)] + [(f"closure@{g}", g) for g in gains]:
+            use = g is not None
             rows = []
             with Context(nc, nc, nc) as cc:
                 _set_state_dev(cc, uci.data_ptr(), bci.data_ptr())
-                corr = cl.Corrector(net, nc, gain=gain) if use else None
+                corr = cl.Corrector(net, nc, gain=g) if use else None
                 nst, wall = 0, 0.0
                 for hi, tf in enumerate(t_of):
                     cap = 100000 if not use else 4 * out["plain"]["per_horizon"][hi]["steps"] + 64
@@ -435,6 +438,7 @@ def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossi
                         "fallbacks": corr.fallback_count() if corr else 0,
                     })
             out[label] = {"per_horizon": rows, "wall_ms": wall, "steps": nst}
+        out["closure"] = out[f"closure@{gains[0]}"]
         out["speedup_vs_fine"] = out["fine_ms"] / max(out["closure"]["wall_ms"], 1e-9)
         res.append(out)
         if log:
@@ -454,8 +458,23 @@ def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossi
     summary["fallback_rate"] = float(np.sum([r["closure"]["per_horizon"][-1]["fallbacks"] for r in res]) /
                                      max(1, np.sum([r["closure"]["steps"] for r in res])))
     summary["speedup_vs_fine"] = float(np.mean([r["speedup_vs_fine"] for r in res]))
-    return {"seeds": list(seeds), "fine": fine, "coarse": nc, "horizons": horizons, "gain": gain,
-            "summary": summary, "runs": res}
+    # every gain: the mean of each error over the seeds at every horizon, and the
+    # fraction of seeds where it is below the plain coarse run's
+    scan = {}
+    for g in gains:
+        lab = f"closure@{g}"
+        e = {}
+        for hi, h in enumerate(horizons):
+            for k in keys:
+                v = [r[lab]["per_horizon"][hi][k] for r in res]
+                pv = [r["plain"]["per_horizon"][hi][k] for r in res]
+                e[f"{k}@{h}"] = float(np.mean(v))
+                e[f"{k}@{h}_wins"] = float(np.mean([a < b for a, b in zip(v, pv)]))
+        e["fallback_rate"] = float(np.sum([r[lab]["per_horizon"][-1]["fallbacks"] for r in res]) /
+                                   max(1, np.sum([r[lab]["steps"] for r in res])))
+        scan[str(g)] = e
+    return {"seeds": list(seeds), "fine": fine, "coarse": nc, "horizons": horizons, "gain": gains[0],
+            "gains": gains, "summary": summary, "gain_scan": scan, "runs": res}
 
 
 def main(argv=None):
@@ -471,6 +490,8 @@ def main(argv=None):
     ap.add_argument("--eval-seeds", type=int, nargs="*", default=list(range(1000, 1008)))
     ap.add_argument("--crossings", type=float, nargs="+", default=[0.5, 1.0, 2.0])
     ap.add_argument("--gain", type=float, default=1.0, help="scale of the applied correction")
+    ap.add_argument("--gains", type=float, nargs="*", default=None,
+                    help="evaluate every one of these scales (the first is reported as the closure)")
     ap.add_argument("--model", default="closure_model.npz")
     ap.add_argument("--load", default=None, help="start from this model (evaluate it, or fine-tune it)")
     ap.add_argument("--onpolicy", type=int, default=0,
@@ -508,10 +529,11 @@ def main(argv=None):
         report["stats"] = stats.to_json()
         net.save(a.model)
         del ds
-    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings, gain=a.gain)
+    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings, gain=a.gain, gains=a.gains)
     with open(a.report, "w") as f:
         json.dump(report, f, indent=1)
     print(json.dumps(report["evaluation"]["summary"]))
+    print(json.dumps(report["evaluation"]["gain_scan"]))
 
 
 if __name__ == "__main__":
