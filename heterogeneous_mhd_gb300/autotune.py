@@ -68,6 +68,11 @@ def candidates(n: int):
     if n % 8 == 0 and 8 <= n // 8 <= 64 and (n // 8) & (n // 8 - 1) == 0:
         fx += [{"fluidx.threads": t, "fluidx.cells": 8} for t in (32, 64, 128, 256) if t >= n // 8]
     adv = []
+    if n in (64, 128, 256):  # the warp-per-pencil kernel
+        for j in (2, 4):
+            for k in (4, 8, 16, 32):
+                if n % j == 0 and n % k == 0:
+                    adv.append({"advect.kernel": 6, "advect.J": j, "advect.K": k})
     if n % 4 == 0 and n % 32 == 0:  # the x-walking kernel
         for xk in (2, 4, 8):
             for slots in (2, 3):

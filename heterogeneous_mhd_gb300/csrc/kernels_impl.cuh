@@ -9,6 +9,7 @@
 #include "mhd_advect3.cuh"
 #include "mhd_advect4.cuh"
 #include "mhd_advect5.cuh"
+#include "mhd_advect6.cuh"
 #include "mhd_fluidx2.cuh"
 #include "mhd_launch.h"
 #include "mhd_tmap.h"
@@ -110,6 +111,8 @@ static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
             e = encode_map_3d(&tm.bn_in, a.ub, 3ull * a.nx, ny, nz, 4, by, bz);
         if (e == cudaSuccess)
             e = encode_map_3d(&tm.u_out, a.u_out, 5ull * a.nx, ny, nz, 5 * kSweepP, by, bz);
+        if (e == cudaSuccess && a.w_out)
+            e = encode_map_3d(&tm.w_out, a.w_out, 2ull * a.nx, ny, nz, 2 * kSweepP, by, bz);
         if (e != cudaSuccess)
             return e;
         smem = fluidx_sweep_smem_bytes(n);
@@ -153,7 +156,8 @@ static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
         FxPlan p;
         const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.uu) |
                              reinterpret_cast<uintptr_t>(a.ub);
-        if (a.cfl_part || a.w_out || (al & 15) != 0 ||
+        if (a.cfl_part || (a.w_out && (a.w_comp < 1 || a.w_comp > 3 || (reinterpret_cast<uintptr_t>(a.w_out) & 15))) ||
+            (al & 15) != 0 ||
             !plan_fluidx_sweep(a.axis == 1 ? a.ny : a.nz, a.nx, a.bs.count, p))
             return cudaErrorInvalidValue;
         return (a.axis == 1) ? fluidx_sweep<1>(a, p, s) : fluidx_sweep<2>(a, p, s);
@@ -233,7 +237,7 @@ struct A3Plan {
     int C, T, NS, J, K;
 };
 
-static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax = 0, int uc = 5)
+static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax = 0, int uc = 5, int boxes = 1)
 {
     if (!kV2 || !aligned)
         return false;
@@ -262,7 +266,8 @@ static bool plan_advect3(int nx, int ny, int nz, bool aligned, A3Plan& p, int ax
     for (int k = 1; k <= nz && k <= 64; k++) {
         if (nz % k != 0)
             continue;
-        if (kt ? (k == kt) : ((long long)(ny / p.J) * (nz / k) >= 4LL * ctas * 152 && k <= 32))
+        // the launch's CTAs are the boxes' together (a batch class is one launch)
+        if (kt ? (k == kt) : ((long long)(ny / p.J) * (nz / k) * boxes >= 4LL * ctas * 152 && k <= 32))
             p.K = k;
     }
     return true;
@@ -402,6 +407,81 @@ static cudaError_t advect_x4(const AdvectArgs& a, const A4Plan& p, cudaStream_t 
     return cudaErrorInvalidValue;
 }
 
+// Warp-per-pencil marching kernel (FP32, the x sweep with the side array,
+// b(1) read in place, one box): pencils of n = 32 C cells (C = 2, 4, 8), J
+// pencils per CTA (2, or 4 by advect.J), K planes per CTA (the largest that
+// gives >= 4 waves, or advect.K).  The planner's choice for pencils of 128
+// and 256 cells (at 256^3 it measured 134 against 184 us for the marching
+// kernel), and by advect.kernel = 6 for 64.
+struct A6Plan {
+    int C, J, K;
+};
+
+static bool plan_advect6(const AdvectArgs& a, bool aligned, A6Plan& p)
+{
+    const int kn = tune_value(TUNE_ADVECT_KERNEL);
+    if (!kV2 || !aligned || a.axis != 0 || !(kn == 6 || (kn == 0 && (a.nx == 128 || a.nx == 256))))
+        return false;
+    if (a.w == nullptr || (reinterpret_cast<uintptr_t>(a.w) & 15) != 0 || a.b1_src != a.ub || a.bs.count != 1)
+        return false;
+    if (a.nx % 32 != 0 || !(a.nx / 32 == 2 || a.nx / 32 == 4 || a.nx / 32 == 8))
+        return false;
+    p.C = a.nx / 32;
+    const int jt = tune_value(TUNE_ADVECT_J);
+    p.J = (jt == 4) ? 4 : 2;  // two pencils per CTA measured best at 256^3 (134 against 150 us)
+    if (a.ny % p.J != 0)
+        return false;
+    const int ctas = advect6_min_ctas(p.J);
+    const int kt = tune_value(TUNE_ADVECT_K);
+    p.K = 0;
+    for (int k = 1; k <= a.nz && k <= 64; k++) {
+        if (a.nz % k != 0)
+            continue;
+        if (kt ? (k == kt) : ((long long)(a.ny / p.J) * (a.nz / k) * a.bs.count >= 4LL * ctas * 152 || k == 1))
+            p.K = k;
+    }
+    return p.K != 0;
+}
+
+template <int C, int J>
+static cudaError_t launch_ad6(const AdvectArgs& a, int K, cudaStream_t s)
+{
+    // swizzled side-array rows (one box) for 8 and 4 cells per lane
+    constexpr bool SW = (C == 8 || C == 4);
+    static bool attr = false;
+    cudaError_t e = allow_smem(k_advect6<EX, C, J, SW>, attr, true);
+    if (e != cudaSuccess)
+        return e;
+    AdvectArgs b = a;
+    b.P = J;
+    b.K = K;
+    CUtensorMap wmap{};
+    if constexpr (SW) {
+        if (a.bs.count != 1)
+            return cudaErrorInvalidValue;
+        e = encode_map_2d(&wmap, a.w, 2 * C, (uint64_t)a.nx * a.ny * a.nz / C, 32,
+                          C == 8 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+        if (e != cudaSuccess)
+            return e;
+    }
+    dim3 grid(a.ny / J, a.nz / K, a.bs.count);
+    k_advect6<EX, C, J, SW><<<grid, advect6_threads(J), advect6_smem_bytes(C * 32, J), s>>>(b, wmap);
+    return cudaGetLastError();
+}
+
+static cudaError_t advect_x6(const AdvectArgs& a, const A6Plan& p, cudaStream_t s)
+{
+    switch (p.C * 10 + p.J) {
+    case 82: return launch_ad6<8, 2>(a, p.K, s);
+    case 84: return launch_ad6<8, 4>(a, p.K, s);
+    case 42: return launch_ad6<4, 2>(a, p.K, s);
+    case 44: return launch_ad6<4, 4>(a, p.K, s);
+    case 22: return launch_ad6<2, 2>(a, p.K, s);
+    case 24: return launch_ad6<2, 4>(a, p.K, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
 // Sweep-walking kernel of the fused step's sweeps along y and z (FP32, one
 // box): lanes along x (nx a multiple of 32), KT planes per CTA (4 by default,
 // or sweep.k), NS chunk buffers (3, or 2 by sweep.slots), the pencil length a
@@ -415,6 +495,8 @@ static bool plan_advect5(const AdvectArgs& a, A4Plan& p)
                          reinterpret_cast<uintptr_t>(a.ub);
     if ((al & 15) != 0 || a.nx % kA5J != 0 || n % kA4X != 0)
         return false;
+    if ((long long)a.nx * a.ny * a.nz * 5 >= (1LL << 31))  // 32-bit offsets inside the box
+        return false;
     const int kt = tune_value(TUNE_SWEEP_K);
     p.NS = (tune_value(TUNE_SWEEP_SLOTS) == 2) ? 2 : 3;
     p.KT = 0;
@@ -424,15 +506,15 @@ static bool plan_advect5(const AdvectArgs& a, A4Plan& p)
     return p.KT != 0;
 }
 
-template <int KT, int NS, int AX>
+template <int KT, int NS, int AX, bool WU = false>
 static cudaError_t launch_ad5(const AdvectArgs& a, cudaStream_t s)
 {
     static bool attr = false;
     static int per_sm_of[kMaxOccDevices] = {}, nsm_of[kMaxOccDevices] = {};
-    cudaError_t e = allow_smem(k_advect5<EX, KT, NS, AX>, attr, true);
+    cudaError_t e = allow_smem(k_advect5<EX, KT, NS, AX, WU>, attr, true);
     if (e != cudaSuccess)
         return e;
-    const size_t smem = advect5_smem_bytes(KT, NS);
+    const size_t smem = advect5_smem_bytes(KT, NS, WU);
     int dev = 0;
     e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
@@ -444,8 +526,8 @@ static cudaError_t launch_ad5(const AdvectArgs& a, cudaStream_t s)
     if (!per_sm) {
         e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect5<EX, KT, NS, AX>, advect5_threads(KT),
-                                                              smem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_advect5<EX, KT, NS, AX, WU>,
+                                                              advect5_threads(KT), smem);
         if (e != cudaSuccess)
             return e;
         if (per_sm < 1)
@@ -457,22 +539,31 @@ static cudaError_t launch_ad5(const AdvectArgs& a, cudaStream_t s)
     const long long cap = (work / 8 > 0) ? work / 8 : 1;
     if (ctas > cap)
         ctas = cap;
-    k_advect5<EX, KT, NS, AX><<<dim3((unsigned)ctas, 1, 1), advect5_threads(KT), smem, s>>>(a);
+    k_advect5<EX, KT, NS, AX, WU><<<dim3((unsigned)ctas, 1, 1), advect5_threads(KT), smem, s>>>(a);
     return cudaGetLastError();
 }
 
+template <int AX, bool WU>
+static cudaError_t advect_y5_w(const AdvectArgs& a, const A4Plan& p, cudaStream_t s)
+{
+    switch (p.KT * 10 + p.NS) {
+    case 82: return launch_ad5<8, 2, AX, WU>(a, s);
+    case 83: return launch_ad5<8, 3, AX, WU>(a, s);
+    case 42: return launch_ad5<4, 2, AX, WU>(a, s);
+    case 43: return launch_ad5<4, 3, AX, WU>(a, s);
+    case 22: return launch_ad5<2, 2, AX, WU>(a, s);
+    case 23: return launch_ad5<2, 3, AX, WU>(a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// the (rho, m_d) side array of the fluidx before, when given, replaces u in the rows
 template <int AX>
 static cudaError_t advect_y5(const AdvectArgs& a, const A4Plan& p, cudaStream_t s)
 {
-    switch (p.KT * 10 + p.NS) {
-    case 82: return launch_ad5<8, 2, AX>(a, s);
-    case 83: return launch_ad5<8, 3, AX>(a, s);
-    case 42: return launch_ad5<4, 2, AX>(a, s);
-    case 43: return launch_ad5<4, 3, AX>(a, s);
-    case 22: return launch_ad5<2, 2, AX>(a, s);
-    case 23: return launch_ad5<2, 3, AX>(a, s);
-    }
-    return cudaErrorInvalidValue;
+    if (a.w != nullptr && (reinterpret_cast<uintptr_t>(a.w) & 15) == 0)
+        return advect_y5_w<AX, true>(a, p, s);
+    return advect_y5_w<AX, false>(a, p, s);
 }
 
 template <int C, int T>
@@ -507,6 +598,9 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
     const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
                          reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
     if constexpr (kV2) {
+        A6Plan p6;
+        if (plan_advect6(a, (al & 15) == 0, p6))
+            return advect_x6(a, p6, s);
         A4Plan p4;
         if (plan_advect4(a, (al & 15) == 0, p4))
             return advect_x4(a, p4, s);
@@ -514,12 +608,12 @@ static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
         const bool wu = a.w != nullptr && (reinterpret_cast<uintptr_t>(a.w) & 15) == 0 &&
                         (a.bs.count == 1 || a.bs.w % 16 == 0);
         A3Plan p3;
-        if (wu && plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3, 0, 2) && p3.C == 4) {
+        if (wu && plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3, 0, 2, a.bs.count) && p3.C == 4) {
             a.P = p3.J;
             a.K = p3.K;
             return (p3.NS == 2) ? launch_ad3_t<4, 2, 0, true>(a, p3.T, s) : launch_ad3_t<4, 3, 0, true>(a, p3.T, s);
         }
-        if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3)) {
+        if (plan_advect3(a.nx, a.ny, a.nz, (al & 15) == 0, p3, 0, 5, a.bs.count)) {
             a.P = p3.J;
             a.K = p3.K;
             if (p3.C == 4)
@@ -663,8 +757,17 @@ static int transpose_writes_w(int axis, int nx, int ny, int nz)
     return kV2 && nx % kT3 == 0 && na % kT3 == 0;
 }
 
+// nonzero if the fused step's fluidx sweep along `axis` (1: y, 2: z) of this
+// grid writes the side array when asked
+static int sweep_writes_w(int axis, int nx, int ny, int nz)
+{
+    FxPlan p;
+    return kV2 && (axis == 1 || axis == 2) && plan_fluidx_sweep(axis == 1 ? ny : nz, nx, 1, p);
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
-                               sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w, transpose_writes_w};
+                               sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w, transpose_writes_w,
+                               sweep_writes_w};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

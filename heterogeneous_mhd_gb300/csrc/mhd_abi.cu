@@ -319,7 +319,7 @@ extern "C" MHD_API int mhd_sync(mhd_ctx* c)
 // ------------------------------------------------------------ operators
 
 static int op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx, int ny, int nz, double dt,
-                     const void* dt_dev, void* cfl_part, int axis = 0, void* w_out = nullptr)
+                     const void* dt_dev, void* cfl_part, int axis = 0, void* w_out = nullptr, int w_comp = 1)
 {
     MHD_TRY(check_dims(nx, ny, nz));
     FluidxArgs a{};
@@ -339,6 +339,7 @@ static int op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx
     a.err = c->err_dev;
     a.axis = axis;
     a.w_out = w_out;
+    a.w_comp = w_comp;
     KTimer kt(c, MHD_K_FLUIDX);
     CUDA_TRY(c->ks->fluidx(a, c->stream));
     return MHD_OK;
@@ -706,23 +707,30 @@ static int enqueue_fused_step(mhd_ctx* c, double cfl)
     const int nx = c->nx, ny = c->ny, nz = c->nz;
     void *U0 = c->U[0].p, *U1 = c->U[1].p, *B0 = c->B[0].p, *B1 = c->B[1].p;
     const void* dt = static_cast<char*>(c->clock.p) + 2 * c->elem;
+    // Every fluidx but the last writes the side array the advectbyzx after it
+    // reads: rho and the momentum along that advectbyzx's sweep (1 m_x, 2 m_y,
+    // 3 m_z), 8 instead of 20 bytes per cell.
+    const bool al = ((size_t)nx * 5 * c->elem) % 16 == 0 && ((size_t)nx * 3 * c->elem) % 16 == 0;
+    void* Wx = (c->W.p && c->ks->fluidx_writes_w(nx, ny, nz, al ? 1 : 0)) ? c->W.p : nullptr;
+    void* Wy = (c->W.p && c->ks->sweep_writes_w(1, nx, ny, nz)) ? c->W.p : nullptr;
+    void* Wz = (c->W.p && c->ks->sweep_writes_w(2, nx, ny, nz)) ? c->W.p : nullptr;
     MHD_TRY(op_finalize(c, c->part.p, c->clock.p, c->cfl_nparts, U0, B0, nx, ny, nz, cfl, 1));
     // x
-    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 0));
-    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 0));
+    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 0, Wx));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 0, Wx));
     // y
-    MHD_TRY(op_fluidx(c, U0, U1, B1, nx, ny, nz, 0, dt, nullptr, 1));
-    MHD_TRY(op_advect(c, B0, B1, U0, B1, nx, ny, nz, 0, dt, 1));
+    MHD_TRY(op_fluidx(c, U0, U1, B1, nx, ny, nz, 0, dt, nullptr, 1, Wy, 2));
+    MHD_TRY(op_advect(c, B0, B1, U0, B1, nx, ny, nz, 0, dt, 1, Wy));
     // z, z
-    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 2));
-    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 2));
-    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 2));
-    MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, nullptr, 2));
+    MHD_TRY(op_fluidx(c, U1, U0, B0, nx, ny, nz, 0, dt, nullptr, 2, Wz, 3));
+    MHD_TRY(op_advect(c, B1, B0, U1, B0, nx, ny, nz, 0, dt, 2, Wz));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 2, Wz));
+    MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, nullptr, 2, Wz, 2));
     // y
-    MHD_TRY(op_advect(c, B1, B0, U0, B0, nx, ny, nz, 0, dt, 1));
-    MHD_TRY(op_fluidx(c, U1, U0, B1, nx, ny, nz, 0, dt, nullptr, 1));
+    MHD_TRY(op_advect(c, B1, B0, U0, B0, nx, ny, nz, 0, dt, 1, Wz));
+    MHD_TRY(op_fluidx(c, U1, U0, B1, nx, ny, nz, 0, dt, nullptr, 1, Wy, 1));
     // x, with the calcfl epilogue for the next step
-    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0));
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0, Wy));
     const size_t nparts = fluidx_parts(c);
     if (c->part.cap < nparts * c->ks->part_bytes)
         return MHD_ERR_ARG;

@@ -44,40 +44,52 @@ constexpr int kA5UROW = kA5UHR + 4;      // staged u row (left halo rho, m_d, 2 
 constexpr int kA5BHR = 3 * 32;           // b of the right halo cell x0+32
 constexpr int kA5BROW = kA5BHR + 4;      // staged b row (32 records | halo + 1 pad)
 
+// With the side array (WU): a staged u row holds (rho, m_d) only: left halo
+// rho, m_d, 2 pad | 32 pairs | right halo rho, m_d, 2 pad
+constexpr int kA5WIN = 4;                 // first float of the 32 staged pairs
+constexpr int kA5WHR = kA5WIN + 2 * 32;   // rho, m_d of the right halo cell x0+32
+constexpr int kA5WROW = kA5WHR + 4;
+
 __host__ __device__ inline int advect5_threads(int KT) { return (KT + 1) * 32; }
 
-__host__ __device__ inline size_t advect5_smem_bytes(int KT, int NS)
+__host__ __device__ inline size_t advect5_smem_bytes(int KT, int NS, bool wu = false)
 {
-    const size_t buf = (size_t)(KT + 2) * kA4X * kA5UROW + (size_t)(KT + 1) * kA4X * kA5BROW;
+    const size_t buf = (size_t)(KT + 2) * kA4X * (wu ? kA5WROW : kA5UROW) + (size_t)(KT + 1) * kA4X * kA5BROW;
     return (NS * buf + 4 * ((size_t)(KT + 1) * 32 + KT)) * sizeof(float);
 }
 
-template <bool EX, int KT, int NS, int AX>
+// WU: the u rows come from the (rho, m_d) side array a.w that the fluidx
+// before wrote (8 instead of 20 bytes per cell staged and read)
+template <bool EX, int KT, int NS, int AX, bool WU = false>
 __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_advect5(AdvectArgs a)
 {
     static_assert(AX == 1 || AX == 2, "sweeps along y or z");
     static_assert(NS == 2 || NS == 3, "two or three chunk buffers");
     select_box(a, blockIdx.z);
     constexpr int NW = KT + 1;
-    constexpr int PU = kA4X * kA5UROW, PB = kA4X * kA5BROW;  // one staged plane (four rows)
+    // staged u row: first record, right halo, length, floats per record (rho at 0)
+    constexpr int UIN = WU ? kA5WIN : kA5UIN, UHR = WU ? kA5WHR : kA5UHR, UROW = WU ? kA5WROW : kA5UROW;
+    constexpr int REC = WU ? 2 : 5, UPR = WU ? 16 : 40;       // floats per record, 16-byte pieces per row
+    constexpr int PU = kA4X * UROW, PB = kA4X * kA5BROW;      // one staged plane (four rows)
     constexpr int UBUF = (KT + 2) * PU, BBUF = (KT + 1) * PB;
-    constexpr int MD = sweep_u<AX>(1);                                   // the sweep momentum
+    constexpr int MD = WU ? 1 : sweep_u<AX>(1);                          // the sweep momentum in a record
     constexpr int CD = sweep_b<AX>(0), CJ = sweep_b<AX>(1), CK = sweep_b<AX>(2);
     extern __shared__ __align__(16) float a5_smem[];
-    float* Us = a5_smem;                                      // [NS][KT+2][4][kA5UROW]
+    float* Us = a5_smem;                                      // [NS][KT+2][4][UROW]
     float* Bs = Us + NS * UBUF;                               // [NS][KT+1][4][kA5BROW]
     float4* FBx = reinterpret_cast<float4*>(Bs + NS * BBUF);  // [KT+1][32]
     float4* FAx = FBx + NW * 32;                              // [KT]
 
+    // offsets in floats fit 32 bits: the planner takes boxes of fewer than 2^31 / 5 cells
     const int nx = a.nx, ny = a.ny;
     const int n = (AX == 1) ? a.ny : a.nz;    // positions along the walk (pencil length)
     const int nk = (AX == 1) ? a.nz : a.ny;   // planes
-    const long long di = (AX == 1) ? (long long)nx : (long long)nx * ny;  // cells between walk positions
-    const long long dk = (AX == 1) ? (long long)nx * ny : (long long)nx;  // cells between planes
+    const int di = (AX == 1) ? nx : nx * ny;  // cells between walk positions
+    const int dk = (AX == 1) ? nx * ny : nx;  // cells between planes
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const bool bw = (w == KT);
     const float dt = load_dt<float>(a.dt_ptr, a.dt_val);
-    const float* uu = static_cast<const float*>(a.uu);
+    const float* uu = static_cast<const float*>(WU ? a.w : a.uu);  // what the u rows hold
     const float* ub = static_cast<const float*>(a.ub);
     const float* b1s = static_cast<const float*>(a.b1_src);
     float* bo = static_cast<float*>(a.b_out);
@@ -88,18 +100,18 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
     const int ka = bw ? (lane < KT ? lane : 0) : w;  // plane in the tile of the A row
     int rAm, mAm, rAc, mAc, rBm, mBm, rBc, mBc, bA, bB;
     if (!bw) {
-        rAc = (w + 1) * PU + kA5UIN + 5 * lane;
-        rAm = (w + 1) * PU + (lane ? kA5UIN + 5 * (lane - 1) : 0);
+        rAc = (w + 1) * PU + UIN + REC * lane;
+        rAm = (w + 1) * PU + (lane ? UIN + REC * (lane - 1) : 0);
         mAm = rAm + (lane ? MD : 1);
-        rBm = w * PU + kA5UIN + 5 * lane;
+        rBm = w * PU + UIN + REC * lane;
         rBc = rAc;
         bA = bB = w * PB + 3 * lane;
     } else {
-        rAm = (ka + 1) * PU + kA5UIN + 5 * 31;
+        rAm = (ka + 1) * PU + UIN + REC * 31;
         mAm = rAm + MD;
-        rAc = (ka + 1) * PU + kA5UHR;
-        rBm = KT * PU + kA5UIN + 5 * lane;
-        rBc = (KT + 1) * PU + kA5UIN + 5 * lane;
+        rAc = (ka + 1) * PU + UHR;
+        rBm = KT * PU + UIN + REC * lane;
+        rBc = (KT + 1) * PU + UIN + REC * lane;
         bA = ka * PB + kA5BHR;
         bB = KT * PB + 3 * lane;
     }
@@ -108,22 +120,21 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
     mBc = rBc + MD;
 
     // copy assignments of this lane inside one staged plane: 16-byte pieces
-    // p = lane + 32 q of the four rows (u: 40 per row, b: 24 per row) and one
-    // 4-byte halo word (u: lanes 0..15, b: lanes 0..11); source offsets in
-    // floats from the plane's first row at x0
-    int uqd[5], uqs[5], bqd[3], bqs[3];
-#pragma unroll
-    for (int q = 0; q < 5; q++) {
-        const int p = lane + 32 * q, r = p / 40, pc = p - 40 * r;
-        uqd[q] = r * kA5UROW + kA5UIN + 4 * pc;
-        uqs[q] = (int)(r * di * 5) + 4 * pc;
-    }
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
+    // p = lane + 32 q of the four rows (u: 40 per row, or 16 of the side
+    // array; b: 24 per row) and one 4-byte halo word (u: lanes 0..15, b: lanes
+    // 0..11); source offsets in floats from the plane's first row at x0
+    // (recomputed per chunk: a few integer operations, which keeps them out of
+    // the registers)
+    auto uq = [&](int q, int& d, int& src) {
+        const int p = lane + 32 * q, r = p / UPR, pc = p - UPR * r;
+        d = r * UROW + UIN + 4 * pc;
+        src = r * di * REC + 4 * pc;
+    };
+    auto bq = [&](int q, int& d, int& src) {
         const int p = lane + 32 * q, r = p / 24, pc = p - 24 * r;
-        bqd[q] = r * kA5BROW + 4 * pc;
-        bqs[q] = (int)(r * di * 3) + 4 * pc;
-    }
+        d = r * kA5BROW + 4 * pc;
+        src = r * di * 3 + 4 * pc;
+    };
     auto kwrap = [&](int k) { return (k < 0) ? k + nk : (k >= nk ? k - nk : k); };
 
     // Work split (as the x-walking kernel): whole tiles in rounds, then the
@@ -153,40 +164,49 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
         const int xl = (x0 == 0) ? nx - 1 : x0 - 1, xh = (x0 + kA5J == nx) ? 0 : x0 + kA5J;
         // halo words of this lane (u: row r, left/right, rho/m_d; b: row r, component)
         const int uh_r = (lane >> 2) & 3, uh_side = (lane >> 1) & 1, uh_word = lane & 1;
-        const int uhd = uh_r * kA5UROW + (uh_side ? kA5UHR : 0) + uh_word;
-        const long long uhs = uh_r * di * 5 + (long long)((uh_side ? xh : xl) - x0) * 5 + (uh_word ? MD : 0);
+        const int uhd = uh_r * UROW + (uh_side ? UHR : 0) + uh_word;
+        const int uhs = uh_r * di * REC + ((uh_side ? xh : xl) - x0) * REC + (uh_word ? MD : 0);
         const int bh_r = lane / 3, bh_c = lane - 3 * bh_r;
         const int bhd = bh_r * kA5BROW + kA5BHR + bh_c;
-        const long long bhs = bh_r * di * 3 + (long long)(xh - x0) * 3 + bh_c;
-        const long long kbu0 = (long long)kwrap(k0 + w - 1) * dk + x0;  // staged u plane w
-        const long long kbu1 = (long long)kwrap(k0 + KT) * dk + x0;     // staged u plane KT+1 (warp 0)
-        const long long kbb = (long long)kwrap(k0 + w) * dk + x0;       // staged b plane w
+        const int bhs = bh_r * di * 3 + (xh - x0) * 3 + bh_c;
+        const int kbu0 = kwrap(k0 + w - 1) * dk + x0;  // staged u plane w
+        const int kbu1 = kwrap(k0 + KT) * dk + x0;     // staged u plane KT+1 (warp 0)
+        const int kbb = kwrap(k0 + w) * dk + x0;       // staged b plane w
 
         // virtual chunk v (c0-1 .. c1, periodic) into ring buffer s
         auto load_chunk = [&](int v, int s) {
             const int xr = (v < 0) ? v + NC : (v >= NC ? v - NC : v);
-            const long long row0 = (long long)(kA4X * xr) * di;
+            const int row0 = kA4X * xr * di;
             float* ud = Us + s * UBUF + w * PU;
-            const float* us = uu + (row0 + kbu0) * 5;
+            const float* us = uu + (row0 + kbu0) * REC;
 #pragma unroll
-            for (int q = 0; q < 5; q++)
-                cp_async16(ud + uqd[q], us + uqs[q]);
+            for (int q = 0; q < 4 * UPR / 32; q++) {
+                int d, src;
+                uq(q, d, src);
+                cp_async16(ud + d, us + src);
+            }
             if (lane < 16)
                 cp_async4(ud + uhd, us + uhs);
             if (w == 0) {  // the last staged u plane (k0 + KT)
                 float* ud1 = Us + s * UBUF + (KT + 1) * PU;
-                const float* us1 = uu + (row0 + kbu1) * 5;
+                const float* us1 = uu + (row0 + kbu1) * REC;
 #pragma unroll
-                for (int q = 0; q < 5; q++)
-                    cp_async16(ud1 + uqd[q], us1 + uqs[q]);
+                for (int q = 0; q < 4 * UPR / 32; q++) {
+                    int d, src;
+                    uq(q, d, src);
+                    cp_async16(ud1 + d, us1 + src);
+                }
                 if (lane < 16)
                     cp_async4(ud1 + uhd, us1 + uhs);
             }
             float* bd = Bs + s * BBUF + w * PB;
             const float* bsrc = ub + (row0 + kbb) * 3;
 #pragma unroll
-            for (int q = 0; q < 3; q++)
-                cp_async16(bd + bqd[q], bsrc + bqs[q]);
+            for (int q = 0; q < 3; q++) {
+                int d, src;
+                bq(q, d, src);
+                cp_async16(bd + d, bsrc + src);
+            }
             if (lane < 12)
                 cp_async4(bd + bhd, bsrc + bhs);
         };
@@ -204,7 +224,7 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
         RB.reset();
         float bdp[4] = {0.f, 0.f, 0.f, 0.f};  // b_d of the chunk before the one read
         // global cell of warp w's pencil at walk position 0
-        const long long cellw = (long long)(k0 + w) * dk + x0 + lane;
+        const int cellw = (k0 + w) * dk + x0 + lane;
         auto chunk = [&](int i, auto sbuf) {
             constexpr int S = decltype(sbuf)::value;
             cp_async_wait<NS - 2>();
@@ -217,7 +237,7 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
             float vxA[4], vxB[4], bvA[4], bvB[4], bd1[4];
 #pragma unroll
             for (int r = 0; r < 4; r++) {
-                const float* Ur = U + r * kA5UROW;
+                const float* Ur = U + r * UROW;
                 const float* Br = Bv + r * kA5BROW;
                 const float rc = Ur[rAc], mc = Ur[mAc];
                 vxA[r] = tvdb_face<float, EX>(Ur[mAm], mc, Ur[rAm], rc);
@@ -245,10 +265,10 @@ __global__ void __launch_bounds__((KT + 1) * 32, advect4_min_ctas(KT, NS)) k_adv
                     }
                     const float4 fbn = FBx[(w + 1) * 32 + lane];
                     const float fbv[4] = {fbn.x, fbn.y, fbn.z, fbn.w};
-                    const long long pos0 = (long long)kA4X * (c0 + i - 2);
+                    const int pos0 = kA4X * (c0 + i - 2);
 #pragma unroll
                     for (int m = 0; m < 4; m++) {
-                        const long long cell = cellw + (pos0 + m) * di;
+                        const int cell = cellw + (pos0 + m) * di;
                         float x = b1_staged ? bdp[m] : b1s[cell * 3 + CD];
                         x = x - FA[m];
                         x = x + fan[m];

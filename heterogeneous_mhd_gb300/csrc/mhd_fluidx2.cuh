@@ -41,9 +41,10 @@ __host__ __device__ inline size_t fluidx2_smem_elems(int n, int P)
 // Tensor maps of one sweep along y or z, encoded by the launcher: u and b of
 // the input state with boxes of P cells along x by the whole pencil, b with a
 // box of four words (the b of cell x0+P and one word after it) for the pencil
-// after the group, and u of the output state.
+// after the group, u of the output state, and (when asked) the (rho, m) side
+// array of the output with boxes of 2P words.
 struct SweepMaps {
-    CUtensorMap u_in, b_in, bn_in, u_out;
+    CUtensorMap u_in, b_in, bn_in, u_out, w_out;
 };
 
 // Sweeps along y and z: P = 4 pencils of n = 4T cells per CTA, n <= 256 (one
@@ -459,8 +460,14 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const
             tma_store_wait_all();
         }
     } else {
-        // pencil-major -> rows (the mapping of the gather, reversed), then one tensor store
+        // pencil-major -> rows (the mapping of the gather, reversed), then one
+        // tensor store.  With a side array: rho and the momentum the next
+        // advectbyzx sweeps with (w_comp) of every cell too, as rows of the
+        // x-major side array (8 bytes per cell) in the dead field buffer, and a
+        // second tensor store.
         __syncthreads();
+        R* const rows_w = sf;  // [n][2P]
+        const int wc = a.w_out ? a.w_comp : 0;
         for (int e = tid; e < n * kSweepP; e += blockDim.x) {
             const int r = e / kSweepP, p = e - r * kSweepP;
             const R* src = su + p * SU + 5 * r;
@@ -468,12 +475,18 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const
 #pragma unroll
             for (int c = 0; c < 5; c++)
                 dst[c] = src[c];
+            if (wc) {
+                rows_w[2 * e] = src[0];
+                rows_w[2 * e + 1] = src[wc];
+            }
         }
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
             const int x0 = blockIdx.x * P, kk = blockIdx.y;
             tma_store_3d(&tm.u_out, 5 * x0, (AX == 1) ? 0 : kk, (AX == 1) ? kk : 0, rows_u);
+            if (wc)
+                tma_store_3d(&tm.w_out, 2 * x0, (AX == 1) ? 0 : kk, (AX == 1) ? kk : 0, rows_w);
             tma_store_commit();
             tma_store_wait_all();
         }

@@ -46,7 +46,9 @@ struct FluidxArgs {
     int* err;
     BoxStrides bs;
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
-    void* w_out;          // optional (FP32, x sweep): (rho, m_x) of the new state, 2 values per cell
+    void* w_out;          // optional (FP32): (rho, m) of the new state, 2 values per cell, x-major:
+                          // m = m_x on the x sweep, on the y/z sweeps the momentum component w_comp
+    int w_comp;           // y/z sweeps: raw component of u written with rho (1 m_x, 2 m_y, 3 m_z)
 };
 
 struct AdvectArgs {
@@ -62,7 +64,8 @@ struct AdvectArgs {
     int K;                // planes per CTA along k for the marching kernel (nz % K == 0)
     BoxStrides bs;
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
-    const void* w;        // optional (FP32, x sweep): (rho, m_x) of update_u, 2 values per cell
+    const void* w;        // optional (FP32): (rho, m_d) of update_u, 2 values per cell, x-major, m_d the
+                          // momentum along the sweep (the fluidx before wrote it)
 };
 
 struct TransposeArgs {

@@ -29,6 +29,8 @@ struct KernelSet {
     int (*fluidx_writes_w)(int nx, int ny, int nz, int aligned);
     // nonzero if the transpose (axis 1 or 2) of this grid writes it (TransposeArgs::w_out)
     int (*transpose_writes_w)(int axis, int nx, int ny, int nz);
+    // nonzero if the fused step's fluidx sweep along `axis` (1: y) writes it
+    int (*sweep_writes_w)(int axis, int nx, int ny, int nz);
 };
 
 const KernelSet* kernels_f32_fast();

@@ -49,4 +49,25 @@ inline cudaError_t encode_map_3d(CUtensorMap* map, const void* base, uint64_t w,
     return (r == CUDA_SUCCESS) ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// A 2-D float tensor map over `rows` rows of w words each (w * 4 bytes a
+// multiple of 16), a box of (w, by) elements, with the given shared-memory
+// swizzle: the 16-byte chunk c of a row lands at chunk c ^ (address bits
+// 7.. of the row) in shared memory, which spreads the rows' chunks over the
+// banks when consecutive rows are read by consecutive lanes.
+inline cudaError_t encode_map_2d(CUtensorMap* map, const void* base, uint64_t w, uint64_t rows, uint32_t by,
+                                 CUtensorMapSwizzle swizzle)
+{
+    const EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn)
+        return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {w, rows};
+    const cuuint64_t strides[1] = {w * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)w, by};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return (r == CUDA_SUCCESS) ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 }  // namespace mhd

@@ -228,7 +228,8 @@ def test_plain_step_long_x_pencils_vs_oracle(mhd, cuda, oracle32):
 @pytest.mark.parametrize("knobs", [{"fluidx.cells": 8, "fluidx.threads": 32}, {"fluidx.cells": 8, "fluidx.threads": 64},
                                    {"advect.kernel": 3}, {"advect.kernel": 3, "advect.cells": 8},
                                    {"advect.kernel": 4, "advect.xk": 2, "advect.slots": 2},
-                                   {"advect.kernel": 4, "advect.xk": 4}])
+                                   {"advect.kernel": 4, "advect.xk": 4},
+                                   {"advect.kernel": 6}, {"advect.kernel": 6, "advect.J": 2, "advect.K": 2}])
 def test_launch_shapes_do_not_change_results(knobs, mhd, cuda):
     """Every launch shape the tuner may pick computes the same numbers: the
     EXACT kernels reproduce the reference checksums of the 64^3 vortex and the
@@ -263,3 +264,25 @@ def test_x_walking_advect_step_exact(kt, ns, mhd, cuda, oracle32):
     finally:
         autotune.apply({})
     assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1])
+
+
+@pytest.mark.parametrize("shape,knobs", [((256, 32, 32), {"advect.kernel": 6}),
+                                         ((256, 32, 32), {"advect.kernel": 6, "advect.J": 2, "advect.K": 8}),
+                                         ((128, 64, 64), {"advect.kernel": 6, "advect.K": 1})])
+def test_warp_pencil_advect_step_exact(shape, knobs, mhd, cuda, oracle32):
+    """Strang steps with the warp-per-pencil advectbyzx forced on the x sweeps
+    (pencils of 256 and 128 cells: 8 and 4 cells per lane): EXACT bit for bit
+    against the oracle after two steps, FAST bit for bit against the default
+    launch shapes after one."""
+    from heterogeneous_mhd_gb300 import autotune
+    u0, b0 = mhd.init_vortex(*shape, seed=4, vscale=1.5)
+    ref = oracle32.strang(u0, b0, *shape, 2)
+    fast_default = run(mhd, u0, b0, shape, 1)
+    try:
+        autotune.apply(knobs)
+        u, b, _ = run(mhd, u0, b0, shape, 2, exact=True)
+        uf, bf, _ = run(mhd, u0, b0, shape, 1)
+    finally:
+        autotune.apply({})
+    assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1])
+    assert bitwise_equal(uf, fast_default[0]) and bitwise_equal(bf, fast_default[1])
