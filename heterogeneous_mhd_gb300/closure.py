@@ -171,6 +171,8 @@ class ClosureNet:
         self.v = torch.zeros_like(self.p)
         self.step_count = 0
         self.stats = stats or Stats()
+        # scale of the applied correction chosen on validation runs (1 = as trained)
+        self.gain = 1.0
         self.wf = [torch.empty(l.cout_pad * l.taps * l.cin_pad, dtype=torch.bfloat16, device=self.dev)
                    for l in LAYERS]
         self.wd = [torch.empty(l.cout_pad * l.taps * l.cin_pad, dtype=torch.bfloat16, device=self.dev)
@@ -304,22 +306,26 @@ class ClosureNet:
         np.savez_compressed(path, params=self.params_numpy(),
                             meta=np.frombuffer(json.dumps({"stats": self.stats.to_json(),
                                                            "layers": [l.__dict__ for l in LAYERS],
-                                                           "steps": self.step_count}).encode(), dtype=np.uint8))
+                                                           "steps": self.step_count,
+                                                           "gain": self.gain}).encode(), dtype=np.uint8))
 
     @staticmethod
     def load(path) -> "ClosureNet":
         with np.load(path) as z:
             params = z["params"]
             meta = json.loads(bytes(z["meta"]).decode())
-        return ClosureNet(params, Stats.from_json(meta["stats"]))
+        net = ClosureNet(params, Stats.from_json(meta["stats"]))
+        net.gain = float(meta.get("gain", 1.0))
+        return net
 
 
 class Corrector:
     """Applies a trained net to one coarse box after each plain step; `gain`
-    scales the correction (1 = as trained)."""
+    scales the correction (1 = as trained; None = the net's calibrated gain)."""
 
-    def __init__(self, net: ClosureNet, n: int, ecap: float = 1e-3, gain: float = 1.0):
+    def __init__(self, net: ClosureNet, n: int, ecap: float = 1e-3, gain: float | None = None):
         t = net.torch
+        gain = net.gain if gain is None else gain
         self.net, self.n, self.ecap, self.gain = net, n, ecap, gain
         self.osc = t.tensor(np.asarray(net.stats.oscale) * gain, dtype=t.float32, device=net.dev)
         nv = n ** 3

@@ -477,6 +477,21 @@ def evaluate(net: cl.ClosureNet, seeds, fine: int = 256, factor: int = 4, crossi
             "gains": gains, "summary": summary, "gain_scan": scan, "runs": res}
 
 
+def pick_gain(evaluation: dict) -> float:
+    """The gain of a scan with the most (horizon, quantity) pairs whose mean
+    error over the seeds is below the plain coarse run's, ties broken by the
+    smallest mean ratio of closure to plain error."""
+    s, horizons = evaluation["summary"], evaluation["horizons"]
+    keys = ("rho_rel_l2", "kinetic_spectrum_err", "magnetic_spectrum_err")
+    best = None
+    for g, e in evaluation["gain_scan"].items():
+        ratios = [e[f"{k}@{h}"] / max(s[f"plain_{k}@{h}"], 1e-30) for h in horizons for k in keys]
+        score = (sum(r < 1.0 for r in ratios), -float(np.mean(ratios)))
+        if best is None or score > best[0]:
+            best = (score, float(g))
+    return best[1]
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--runs", type=int, default=48)
@@ -492,6 +507,9 @@ def main(argv=None):
     ap.add_argument("--gain", type=float, default=1.0, help="scale of the applied correction")
     ap.add_argument("--gains", type=float, nargs="*", default=None,
                     help="evaluate every one of these scales (the first is reported as the closure)")
+    ap.add_argument("--calibrate", action="store_true",
+                    help="keep the best of --gains (on the --eval-seeds, which should be validation seeds) "
+                         "as the model's gain and save the model again")
     ap.add_argument("--model", default="closure_model.npz")
     ap.add_argument("--load", default=None, help="start from this model (evaluate it, or fine-tune it)")
     ap.add_argument("--onpolicy", type=int, default=0,
@@ -529,7 +547,13 @@ def main(argv=None):
         report["stats"] = stats.to_json()
         net.save(a.model)
         del ds
-    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings, gain=a.gain, gains=a.gains)
+    gains = a.gains if a.gains else [net.gain if a.load and a.gain == 1.0 else a.gain]
+    report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings, gains=gains)
+    if a.calibrate and a.gains:
+        net.gain = pick_gain(report["evaluation"])
+        report["calibrated_gain"] = net.gain
+        net.save(a.model)
+        print(f"calibrated gain {net.gain} saved in {a.model}", flush=True)
     with open(a.report, "w") as f:
         json.dump(report, f, indent=1)
     print(json.dumps(report["evaluation"]["summary"]))
