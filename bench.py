@@ -52,17 +52,17 @@ ALG_BYTES = {"fluidx": 52, "advectbyzx": 44, "transpose12": 64, "transpose13": 6
 # What the kernels move on average per launch.  Plain step: the three forward
 # fluidx launches and the two backward transposes also write the (rho, m_x)
 # side array (8 B), and every advectbyzx reads it in place of u (8 B, not 20).
-# Fused step: the x-sweep fluidx and the last y-sweep fluidx write it, and
-# the two x-sweep advectbyzx launches read it.
+# Fused step: every fluidx but the last writes (rho, m_d) for the advectbyzx
+# after it (m_d the momentum along that sweep), and every advectbyzx reads it.
 MOVED_BYTES = {"plain": {"fluidx": 52 + 8 * 3 / 6, "advectbyzx": 32, "transpose12": 64 + 8 / 2,
                          "transpose13": 64 + 8 / 2},
-               "fused": {"fluidx": 52 + 8 * 2 / 6, "advectbyzx": (2 * 32 + 4 * 44) / 6}}
+               "fused": {"fluidx": 52 + 8 * 5 / 6, "advectbyzx": 32}}
 # per-cell bytes of a whole step: the reference's operator sequence (6 fluidx
 # x 52 + 6 advectbyzx x 44 + 4 transposes x 64 + a calcfl 32 = 864), what the
 # fused step's operators move (no transposes: 6 x 52 + 6 x 44 = 576), and the
 # five-pass bound of a step that fuses each sweep's operators (5 x 64 = 320)
 STEP_BYTES = {"plain": 864, "fused": 576, "fused_5pass": 320}
-STEP_MOVED = {"plain": 6 * 52 + 3 * 8 + 6 * 32 + 4 * 64 + 2 * 8, "fused": 6 * 52 + 2 * 8 + 2 * 32 + 4 * 44}
+STEP_MOVED = {"plain": 6 * 52 + 3 * 8 + 6 * 32 + 4 * 64 + 2 * 8, "fused": 6 * 52 + 5 * 8 + 6 * 32}
 METRIC = "cell-updates/s at 256^3 (plain vs fused); closure speedup at matched error"
 
 
@@ -146,7 +146,7 @@ def measured_traffic(kernel: str, n: int, variant: str = "plain"):
         t = json.loads(p.read_text())
     except (OSError, ValueError):
         return None
-    t = t.get(variant, t) if variant in t else (t if variant == "plain" else {})
+    t = t.get(variant, {})
     if t.get("grid") != [n, n, n] or kernel not in t:
         return None
     return t[kernel]["dram_bytes_per_launch"]
