@@ -134,6 +134,7 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
         "mhd_batch_stream": (_vp, [_vp]),
         "mhd_batch_launch_count": (C.c_longlong, [_vp]),
         "mhd_batch_classes": (C.c_int, [_vp]),
+        "mhd_batch_tune_edge": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -548,3 +549,7 @@ class Batch:
 
     def classes(self) -> int:
         return int(lib().mhd_batch_classes(self._h))
+
+    def tune_edge(self, edge: int, key: str, value: int) -> None:
+        """A launch-shape knob for the boxes of one edge only (-1: the global setting)."""
+        _check(lib().mhd_batch_tune_edge(self._h, int(edge), key.encode(), int(value)), "mhd_batch_tune_edge")

@@ -132,6 +132,69 @@ def tune(n: int = 256, steps: int = 3, verbose: bool = False, save: bool = True)
     return best
 
 
+def batch_candidates(n: int):
+    """Launch shapes to try for the boxes of edge n of a batch: the fluidx CTA
+    width and the marching advectbyzx (the batch's kernel; the others need
+    the side array or one box)."""
+    out = [{}]
+    out += [{"fluidx.threads": t} for t in (128, 256)]
+    t = n // 4
+    if n % 4 == 0 and 4 <= t <= 128 and not (t & (t - 1)):
+        for slots in (2, 3):
+            for j in _divisors(n, 1, 8):
+                if (2 * j + 1) * t > 384:
+                    continue
+                for k in (4, 8, 16, 32):
+                    if n % k == 0:
+                        out.append({"advect.kernel": 3, "advect.slots": slots, "advect.J": j, "advect.K": k})
+    return out
+
+
+def tune_batch(bt, cfg, steps: int = 3, verbose: bool = False, min_gain: float = 0.02) -> dict:
+    """Per size class of a batch (`bt`, built from the box table `cfg` of
+    batch_config): time every candidate shape on a batch of that class's
+    boxes alone (the same count and initial states), and set the fastest on
+    `bt` with Batch.tune_edge when it beats the planner's shapes by more than
+    min_gain.  Returns {edge: (knobs, ms per step, ms with the planner)}."""
+    import torch
+
+    from . import Batch, init_batch_box
+
+    edges = sorted({x["n"] for x in cfg})
+    keys = ("fluidx.threads", "advect.kernel", "advect.slots", "advect.J", "advect.K")
+    chosen = {}
+    for edge in edges:
+        boxes = [x for x in cfg if x["n"] == edge]
+        with Batch([edge] * len(boxes)) as one:
+            for i, box in enumerate(boxes):
+                one.set_box(i, *init_batch_box(box))
+            stream = torch.cuda.ExternalStream(one.stream())
+            timed = []
+            for cand in batch_candidates(edge):
+                for k in keys:
+                    one.tune_edge(edge, k, int(cand.get(k, 0)) if cand else -1)
+                one.step(1)
+                one.sync()
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                one.step(steps)
+                ev1.record(stream)
+                ev1.synchronize()
+                ms = ev0.elapsed_time(ev1) / steps
+                timed.append((ms, cand))
+                if verbose:
+                    print(f"batch edge {edge} {cand} {ms:.3f} ms", flush=True)
+        base = timed[0][0]
+        best_ms, best = min(timed, key=lambda r: r[0])
+        if best_ms < base * (1.0 - min_gain):
+            for k in keys:
+                bt.tune_edge(edge, k, int(best.get(k, 0)))
+            chosen[edge] = (best, best_ms, base)
+        else:
+            chosen[edge] = ({}, base, base)
+    return chosen
+
+
 def load(n: int) -> dict | None:
     if not CACHE.exists():
         return None

@@ -943,6 +943,15 @@ static int tune_key(const char* key)
     return -1;
 }
 
+int mhd::tune_index(const char* key) { return tune_key(key); }
+
+int mhd::tune_swap(int key, int value)
+{
+    if (key < 0 || key >= TUNE_COUNT)
+        return 0;
+    return g_tune[key].exchange(value);
+}
+
 extern "C" MHD_API int mhd_tune_set(const char* key, int value)
 {
     const int k = tune_key(key);

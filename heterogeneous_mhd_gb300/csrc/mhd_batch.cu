@@ -35,7 +35,27 @@ struct SizeClass {
     int cfl_nparts = 0;     // partials per box currently held
     size_t ustride = 0;     // bytes between consecutive boxes' u (256-byte aligned)
     size_t bstride = 0;
+    int knobs[TUNE_COUNT];  // launch-shape knobs of this class's launches (-1: the global setting)
+    SizeClass() { std::fill(knobs, knobs + TUNE_COUNT, -1); }
     size_t cells() const { return (size_t)n * n * n; }
+};
+
+// Applies a class's own launch-shape knobs for the duration of its enqueue
+// and puts the global values back afterwards.
+struct ClassKnobs {
+    int saved[TUNE_COUNT];
+    const SizeClass& c;
+    explicit ClassKnobs(const SizeClass& cls) : c(cls)
+    {
+        for (int k = 0; k < TUNE_COUNT; k++)
+            saved[k] = (c.knobs[k] >= 0) ? tune_swap(k, c.knobs[k]) : -1;
+    }
+    ~ClassKnobs()
+    {
+        for (int k = 0; k < TUNE_COUNT; k++)
+            if (c.knobs[k] >= 0)
+                tune_swap(k, saved[k]);
+    }
 };
 
 static size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -259,6 +279,7 @@ static int cfl_first_pass(mhd_batch* b)
 static int enqueue_step(mhd_batch* b, double cfl)
 {
     for (auto& c : b->cls) {
+        const ClassKnobs knobs(c);
         const int n = c.n;
         const BoxStrides bs = strides(b, c);
         void *U0 = c.U[0], *U1 = c.U[1], *B0 = c.B[0], *B1 = c.B[1];
@@ -402,3 +423,23 @@ extern "C" MHD_API void* mhd_batch_stream(mhd_batch* b) { return b ? (void*)b->s
 extern "C" MHD_API long long mhd_batch_launch_count(mhd_batch* b) { return b ? b->launches : -1; }
 
 extern "C" MHD_API int mhd_batch_classes(mhd_batch* b) { return b ? (int)b->cls.size() : -1; }
+
+extern "C" MHD_API int mhd_batch_tune_edge(mhd_batch* b, int edge, const char* key, int value)
+{
+    const int k = tune_index(key);
+    if (!b || k < 0 || value < -1)
+        return MHD_ERR_ARG;
+    int hit = 0;
+    for (auto& c : b->cls)
+        if (c.n == edge) {
+            c.knobs[k] = value;
+            hit = 1;
+        }
+    if (!hit)
+        return MHD_ERR_ARG;
+    if (b->graph) {  // the step graph holds the old launch shapes
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return MHD_OK;
+}

@@ -65,5 +65,10 @@ enum TuneKey : int {
 };
 int tune_value(int key);
 long long tune_generation();  // bumped by every change (captured graphs are rebuilt)
+int tune_index(const char* key);  // the TuneKey of a knob name, -1 if unknown
+// Sets a knob without bumping the generation and returns its previous value:
+// for a caller that applies its own values around its own launches (the
+// batch's per-class shapes) and owns the graphs they are captured into.
+int tune_swap(int key, int value);
 
 }  // namespace mhd

@@ -241,6 +241,10 @@ MHD_API int mhd_batch_time(mhd_batch *batch, int box, double *t, double *dt);
 MHD_API void *mhd_batch_stream(mhd_batch *batch);
 MHD_API long long mhd_batch_launch_count(mhd_batch *batch);
 MHD_API int mhd_batch_classes(mhd_batch *batch);
+/* Launch-shape knob (the names of mhd_tune_set) for the launches of the boxes
+ * of one edge only; -1 returns that knob to the global setting.  No
+ * counterpart in the reference (see mhd_batch_create). */
+MHD_API int mhd_batch_tune_edge(mhd_batch *batch, int edge, const char *key, int value);
 
 /* ------------------------------------------------- initial conditions (host) */
 

@@ -166,3 +166,30 @@ def test_batch_large_classes_vs_oracle(mhd, cuda, oracle32):
                 else:
                     e = rel_l2_fields(u, b, ou, ob)
                     assert max(e.values()) <= 1e-5, (i, e)
+
+
+def test_batch_per_edge_launch_shapes(mhd, cuda):
+    """Launch-shape knobs set for one edge only (mhd_batch_tune_edge) change
+    the kernels' shapes, not the results: the FAST boxes stay bit for bit
+    those of the planner's shapes, and a knob for an edge the batch does not
+    hold is refused."""
+    cfg = mhd.batch_config(6, seed=5, edges=(32, 64))
+    ref, ics = make_batch(mhd, cfg, exact=False)
+    with ref:
+        ref.step(3)
+        ref.sync()
+        want = [ref.get_box(i) for i in range(len(cfg))]
+    bt, _ = make_batch(mhd, cfg, exact=False)
+    with bt:
+        edges = sorted({x["n"] for x in cfg})
+        bt.tune_edge(edges[0], "advect.kernel", 3)
+        bt.tune_edge(edges[0], "advect.K", 4)
+        bt.tune_edge(edges[-1], "advect.J", 1)
+        bt.tune_edge(edges[-1], "fluidx.threads", 128)
+        with pytest.raises(mhd.MhdError):
+            bt.tune_edge(40, "advect.K", 4)
+        bt.step(3)
+        bt.sync()
+        for i in range(len(cfg)):
+            u, b = bt.get_box(i)
+            assert bitwise_equal(u, want[i][0]) and bitwise_equal(b, want[i][1]), i
