@@ -313,14 +313,21 @@ def closure_leg(seeds=(1000, 1001, 1002, 1003), fine=256, factor=4, horizons=(0.
     return out
 
 
-def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3):
+def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3, tune=True):
     """The batched workload: 256 vortex boxes of edge 32..128 with their own
-    beta, Mach and dt, FP32, one graph per step; 50 timed steps."""
+    beta, Mach and dt, FP32, one graph per step; 50 timed steps.  With
+    `tune`, the launch shapes of every size class are timed on that class
+    alone first (autotune.tune_batch) and the fastest is kept per class."""
     cfg = mhd.batch_config(nboxes, seed=rank)
     cells = sum(x["n"] ** 3 for x in cfg)
     bt = mhd.Batch([x["n"] for x in cfg])
     for i, box in enumerate(cfg):
         bt.set_box(i, *mhd.init_batch_box(box))
+    shapes = {}
+    if tune:
+        from heterogeneous_mhd_gb300 import autotune
+        shapes = {str(e): {"knobs": k, "ms": round(ms, 3), "planner_ms": round(b, 3)}
+                  for e, (k, ms, b) in autotune.tune_batch(bt, cfg).items()}
     stream = torch.cuda.ExternalStream(bt.stream())
     bt.step(warmup)
     bt.sync()
@@ -339,7 +346,8 @@ def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3):
                        f"Mach 0.2-1.0, FP32, CFL 0.7, own dt per box",
            "boxes": nboxes, "cells": cells, "size_classes": bt.classes(), "steps": steps,
            "ms_per_step": ms / steps, "value": cells * steps / (ms * 1e-3), "unit": "cell-updates/s",
-           "step_alg_gbs": step_gbs, "step_frac": step_gbs / hbm, "gpu_launches": int(launches)}
+           "step_alg_gbs": step_gbs, "step_frac": step_gbs / hbm, "gpu_launches": int(launches),
+           "launch_shapes_per_edge": shapes or "planner defaults"}
     bt.close()
     return out
 
@@ -541,7 +549,7 @@ def our_arm(args):
         # the batch's launch shapes are the planner's: the tuned single-box knobs do not carry over
         from heterogeneous_mhd_gb300 import autotune
         autotune.apply({})
-        line["batch"] = batch_leg(mhd, torch, rank)
+        line["batch"] = batch_leg(mhd, torch, rank, tune=not args.no_tune)
     if not args.no_closure:
         line["closure"] = closure_leg()
     if world == 1 and not args.no_cpu:
@@ -570,6 +578,28 @@ def ncu_case(args):
         assert ctx.check() == mhd.MHD_OK
 
 
+def ncu_closure_case(args):
+    """A short run of the closure's kernels for ncu captures: three training
+    iterations (forward, loss, backward, AdamW) of the net on 4 boxes of
+    64^3 seeded random inputs and targets, no JSON line."""
+    import torch
+
+    from heterogeneous_mhd_gb300 import closure
+
+    nb, n = 4, 64
+    closure.cl().mhd_cl_use_tcgen05(args.tcgen05)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = (torch.randn((nb, n ** 3 * 16), generator=g, device="cuda") * 0.5).to(torch.bfloat16)
+    t = (torch.randn((nb, n ** 3 * 8), generator=g, device="cuda") * 0.1).to(torch.bfloat16)
+    net = closure.ClosureNet(seed=0)
+    for _ in range(3):
+        net.forward(x, nb, n)
+        net.loss(t, nb, n)
+        net.backward(x, nb, n)
+        net.adamw(1e-4)
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -585,12 +615,17 @@ def main():
     ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure leg")
     ap.add_argument("--no-512", action="store_true", help="skip the 512^3 plain-step leg")
     ap.add_argument("--ncu-case", action="store_true", help="run the short profiling case only")
+    ap.add_argument("--ncu-closure", action="store_true", help="run the short closure profiling case only")
+    ap.add_argument("--tcgen05", type=int, default=1,
+                    help="--ncu-closure: 1 warp-specialised tcgen05 convolution, 2 two-buffer, 0 mma.sync")
     ap.add_argument("--knob", action="append", default=[], help="launch-shape knob key=value for --ncu-case")
     ap.add_argument("--fp64-steps", type=int, default=100, help="steps of the FP64 error leg")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.ncu_case:
+    if args.ncu_closure:
+        ncu_closure_case(args)
+    elif args.ncu_case:
         ncu_case(args)
     elif args.impl == "reference":
         reference_arm(args)
