@@ -171,8 +171,10 @@ class ClosureNet:
         self.v = torch.zeros_like(self.p)
         self.step_count = 0
         self.stats = stats or Stats()
-        # scale of the applied correction chosen on validation runs (1 = as trained)
+        # scale of the applied correction chosen on validation runs (1 = as trained),
+        # and per coarse edge where it was calibrated there
         self.gain = 1.0
+        self.gain_by_edge: dict[int, float] = {}
         self.wf = [torch.empty(l.cout_pad * l.taps * l.cin_pad, dtype=torch.bfloat16, device=self.dev)
                    for l in LAYERS]
         self.wd = [torch.empty(l.cout_pad * l.taps * l.cin_pad, dtype=torch.bfloat16, device=self.dev)
@@ -307,7 +309,10 @@ class ClosureNet:
                             meta=np.frombuffer(json.dumps({"stats": self.stats.to_json(),
                                                            "layers": [l.__dict__ for l in LAYERS],
                                                            "steps": self.step_count,
-                                                           "gain": self.gain}).encode(), dtype=np.uint8))
+                                                           "gain": self.gain,
+                                                           "gain_by_edge": {str(k): v for k, v in
+                                                                            self.gain_by_edge.items()}}).encode(),
+                                            dtype=np.uint8))
 
     @staticmethod
     def load(path) -> "ClosureNet":
@@ -316,7 +321,12 @@ class ClosureNet:
             meta = json.loads(bytes(z["meta"]).decode())
         net = ClosureNet(params, Stats.from_json(meta["stats"]))
         net.gain = float(meta.get("gain", 1.0))
+        net.gain_by_edge = {int(k): float(v) for k, v in meta.get("gain_by_edge", {}).items()}
         return net
+
+    def gain_for(self, n: int) -> float:
+        """The calibrated correction gain for coarse boxes of edge n."""
+        return self.gain_by_edge.get(int(n), self.gain)
 
 
 class Corrector:
@@ -325,7 +335,7 @@ class Corrector:
 
     def __init__(self, net: ClosureNet, n: int, ecap: float = 1e-3, gain: float | None = None):
         t = net.torch
-        gain = net.gain if gain is None else gain
+        gain = net.gain_for(n) if gain is None else gain
         self.net, self.n, self.ecap, self.gain = net, n, ecap, gain
         self.osc = t.tensor(np.asarray(net.stats.oscale) * gain, dtype=t.float32, device=net.dev)
         nv = n ** 3

@@ -547,13 +547,18 @@ def main(argv=None):
         report["stats"] = stats.to_json()
         net.save(a.model)
         del ds
-    gains = a.gains if a.gains else [net.gain if a.load and a.gain == 1.0 else a.gain]
+    nc = a.fine // a.factor
+    gains = a.gains if a.gains else [net.gain_for(nc) if a.load and a.gain == 1.0 else a.gain]
     report["evaluation"] = evaluate(net, a.eval_seeds, a.fine, a.factor, a.crossings, gains=gains)
     if a.calibrate and a.gains:
-        net.gain = pick_gain(report["evaluation"])
-        report["calibrated_gain"] = net.gain
+        # kept per coarse edge; a freshly trained net also takes it as its default
+        g = pick_gain(report["evaluation"])
+        net.gain_by_edge[nc] = g
+        if not a.load:
+            net.gain = g
+        report["calibrated_gain"] = g
         net.save(a.model)
-        print(f"calibrated gain {net.gain} saved in {a.model}", flush=True)
+        print(f"calibrated gain {g} for {nc}^3 boxes saved in {a.model}", flush=True)
     with open(a.report, "w") as f:
         json.dump(report, f, indent=1)
     print(json.dumps(report["evaluation"]["summary"]))

@@ -297,14 +297,15 @@ __device__ __forceinline__ void umma_f16(uint32_t tmem, uint64_t ad, uint64_t bd
                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
 
+// (t0, nt: this thread's index among the nt threads that share the copies)
 template <int CIN>
 __device__ __forceinline__ void tc_load_halo(unsigned char* dst, const bf16* src, int box, int z0, int y0, int x0,
-                                             int n)
+                                             int n, int t0, int nt)
 {
     constexpr int CH = CIN / 8;
     const size_t box0 = (size_t)box * n * n * n;
     // consecutive threads: chunks of one voxel, then x (contiguous rows in HBM)
-    for (int e = threadIdx.x; e < HV * CH; e += blockDim.x) {
+    for (int e = t0; e < HV * CH; e += nt) {
         const int c = e % CH, r = e / CH;
         const int xp = r % HX, r2 = r / HX, yp = r2 % HY, zp = r2 / HY;
         const int gx = wrap(x0 + xp - 1, n), gy = wrap(y0 + yp - 1, n), gz = wrap(z0 + zp - 1, n);
@@ -330,6 +331,55 @@ __device__ __forceinline__ void tc_issue_tile(uint32_t tmem, uint64_t a_desc0, u
                 const uint32_t boff = (uint32_t)(tap * CH + 2 * ks) * COUT * 16;
                 umma_f16(tmem + 32 * p, a_desc0 + (aoff >> 4), b_desc0 + (boff >> 4), idesc, tap | ks);
             }
+}
+
+// The epilogue of one voxel: its COUT accumulators (FP32 bits) to bias + GELU
+// in BF16 (and the pre-activation for the backward pass), or times GELU' of
+// the previous layer's pre-activation (the data gradient).
+template <int COUT, int EPI>
+__device__ __forceinline__ void tc_epilogue_row(const uint32_t (&r)[32], size_t v, const float* __restrict__ bias,
+                                                void* __restrict__ y, bf16* __restrict__ zsave,
+                                                const bf16* __restrict__ zprev)
+{
+    __align__(16) bf16 o1[COUT];
+    __align__(16) bf16 o2[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; c += 2) {
+        const float v0 = __uint_as_float(r[c]), v1 = __uint_as_float(r[c + 1]);
+        if constexpr (EPI == EPI_GELU) {
+            const __nv_bfloat162 zz = __floats2bfloat162_rn(v0 + bias[c], v1 + bias[c + 1]);
+            const float2 zf = __bfloat1622float2(zz);
+            *reinterpret_cast<__nv_bfloat162*>(o2 + c) = zz;
+            *reinterpret_cast<__nv_bfloat162*>(o1 + c) = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
+        } else {
+            const float2 zp = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zprev + v * COUT + c));
+            *reinterpret_cast<__nv_bfloat162*>(o1 + c) =
+                __floats2bfloat162_rn(v0 * gelu_grad(zp.x), v1 * gelu_grad(zp.y));
+        }
+    }
+    uint4* yo = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + v * COUT);
+#pragma unroll
+    for (int k = 0; k < COUT / 8; k++)
+        yo[k] = reinterpret_cast<const uint4*>(o1)[k];
+    if constexpr (EPI == EPI_GELU) {
+        uint4* zo = reinterpret_cast<uint4*>(zsave + v * COUT);
+#pragma unroll
+        for (int k = 0; k < COUT / 8; k++)
+            zo[k] = reinterpret_cast<const uint4*>(o2)[k];
+    }
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                 "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                   "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                   "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 template <int CIN, int COUT, int EPI>
@@ -384,7 +434,7 @@ __global__ void __launch_bounds__(256, 1) k_conv_tc(const bf16* __restrict__ x, 
     if ((long long)blockIdx.x < ntiles) {
         int b_, z_, y_, x_;
         coords(blockIdx.x, b_, z_, y_, x_);
-        tc_load_halo<CIN>(sm, x, b_, z_, y_, x_, n);
+        tc_load_halo<CIN>(sm, x, b_, z_, y_, x_, n, tid, blockDim.x);
     }
     int pbox = 0, pz = 0, py = 0, px = 0;  // the previous tile (its epilogue runs this iteration)
     for (long long it = 0;; it++) {
@@ -407,7 +457,7 @@ __global__ void __launch_bounds__(256, 1) k_conv_tc(const bf16* __restrict__ x, 
             if (next < ntiles) {
                 int b_, z_, y_, x_;
                 coords(next, b_, z_, y_, x_);
-                tc_load_halo<CIN>(sm + (ab ^ 1) * ABYTES, x, b_, z_, y_, x_, n);
+                tc_load_halo<CIN>(sm + (ab ^ 1) * ABYTES, x, b_, z_, y_, x_, n, tid, blockDim.x);
                 asm volatile("cp.async.wait_group 1;" ::: "memory");
             } else {
                 asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -439,33 +489,7 @@ __global__ void __launch_bounds__(256, 1) k_conv_tc(const bf16* __restrict__ x, 
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             const int m = q * 32 + lane, vx = m >> 3, vy = m & 7;
             const size_t v = (((size_t)pbox * n + pz + pl) * n + (py + vy)) * n + (px + vx);
-            __align__(16) bf16 o1[COUT];
-            __align__(16) bf16 o2[COUT];
-#pragma unroll
-            for (int c = 0; c < COUT; c += 2) {
-                const float v0 = __uint_as_float(r[c]), v1 = __uint_as_float(r[c + 1]);
-                if constexpr (EPI == EPI_GELU) {
-                    const __nv_bfloat162 zz = __floats2bfloat162_rn(v0 + bias[c], v1 + bias[c + 1]);
-                    const float2 zf = __bfloat1622float2(zz);
-                    *reinterpret_cast<__nv_bfloat162*>(o2 + c) = zz;
-                    *reinterpret_cast<__nv_bfloat162*>(o1 + c) = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
-                } else {
-                    const float2 zp =
-                        __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zprev + v * COUT + c));
-                    *reinterpret_cast<__nv_bfloat162*>(o1 + c) =
-                        __floats2bfloat162_rn(v0 * gelu_grad(zp.x), v1 * gelu_grad(zp.y));
-                }
-            }
-            uint4* yo = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + v * COUT);
-#pragma unroll
-            for (int k = 0; k < COUT / 8; k++)
-                yo[k] = reinterpret_cast<const uint4*>(o1)[k];
-            if constexpr (EPI == EPI_GELU) {
-                uint4* zo = reinterpret_cast<uint4*>(zsave + v * COUT);
-#pragma unroll
-                for (int k = 0; k < COUT / 8; k++)
-                    zo[k] = reinterpret_cast<const uint4*>(o2)[k];
-            }
+            tc_epilogue_row<COUT, EPI>(r, v, bias, y, zsave, zprev);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -478,6 +502,171 @@ __global__ void __launch_bounds__(256, 1) k_conv_tc(const bf16* __restrict__ x, 
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+}
+
+// The same convolution as a warp-specialised pipeline, so that the tensor
+// core does not wait for the epilogue or for the halo loads.  Nine warps:
+//   * warps 0-3 load halo tiles by cp.async into a ring of NA shared buffers
+//     (a stage is announced on a_full once its copies have landed, with one
+//     stage of lag so that two tiles' loads are in flight);
+//   * warp 4 (one elected lane) issues a tile's 2 x 27 x CIN/16 MMAs into
+//     one of NT TMEM stages of 64 columns as soon as its halo is in and the
+//     stage is free, then commits them to a_empty (the halo buffer is free)
+//     and t_full (the accumulators are ready);
+//   * warps 5-8 run the epilogue of a TMEM stage (warp w reads lanes
+//     32 (w % 4).. of both planes) and free the stage on t_empty as soon as
+//     its accumulators are in registers.
+// The weights stay resident.  Every wait is bounded: on timeout the role
+// records DEVERR_TIMEOUT and leaves its loop, the others then time out in
+// turn, and the CTA frees its TMEM after its last MMAs have completed.
+constexpr int kTc2Load = 4;                  // loader warps
+constexpr int kTc2Warps = kTc2Load + 1 + 4;  // + the MMA warp + four epilogue warps
+constexpr int kTc2NT = 4;                    // TMEM stages (4 x 64 = 256 columns)
+
+template <int CIN>
+__host__ __device__ constexpr int tc2_stages() { return CIN >= 32 ? 3 : 4; }  // halo buffers: 3 x 45 KB + 54 KB of weights
+
+template <int CIN, int COUT>
+__host__ __device__ constexpr size_t tc2_smem_bytes()
+{
+    return (size_t)tc2_stages<CIN>() * (CIN / 8) * kChunkBytes + (size_t)27 * (CIN / 8) * COUT * 16 + 1024;
+}
+
+__device__ __forceinline__ void mbar_arrive1(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mhd::smem_u32(bar)) : "memory");
+}
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(kTc2Warps * 32, 1)
+    k_conv_tc2(const bf16* __restrict__ x, const bf16* __restrict__ w, const float* __restrict__ bias,
+               void* __restrict__ y, bf16* __restrict__ zsave, const bf16* __restrict__ zprev, int n, long long ntiles,
+               int* err)
+{
+    static_assert(COUT == 32, "one tile's accumulators are 2 x 32 TMEM columns");
+    constexpr int CH = CIN / 8, NA = tc2_stages<CIN>(), NT = kTc2NT;
+    constexpr int KC = 27 * CH;                  // K chunks of the weights
+    constexpr uint32_t ABYTES = CH * kChunkBytes;
+    constexpr int MMA_WARP = kTc2Load, LOADERS = kTc2Load * 32;
+    extern __shared__ __align__(16) unsigned char tc2_raw[];
+    // 1024-byte aligned start, as an offset from the shared array
+    unsigned char* const sm =
+        tc2_raw + ((1024u - (static_cast<uint32_t>(__cvta_generic_to_shared(tc2_raw)) & 1023u)) & 1023u);
+    unsigned char* const sW = sm + NA * ABYTES;  // [KC][COUT][16 B]
+    __shared__ __align__(8) uint64_t a_full[NA], a_empty[NA], t_full[NT], t_empty[NT];
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int e = tid; e < KC * COUT; e += blockDim.x) {
+        const int co = e % COUT, kc = e / COUT;
+        cp_async16(sW + ((size_t)kc * COUT + co) * 16, w + (size_t)co * 27 * CIN + kc * 8);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async writes -> tensor core
+    if (tid == 0) {
+        for (int i = 0; i < NA; i++) {
+            mhd::mbar_init(&a_full[i], LOADERS);
+            mhd::mbar_init(&a_empty[i], 1);
+        }
+        for (int i = 0; i < NT; i++) {
+            mhd::mbar_init(&t_full[i], 1);
+            mhd::mbar_init(&t_empty[i], 4);
+        }
+    }
+    if (warp == MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+                         mhd::smem_u32(&tmem_base)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    const int tx = n / TCX, ty = n / TCY, tz = n / TCZ;
+    auto coords = [&](long long t, int& box, int& z0, int& y0, int& x0) {
+        x0 = (int)(t % tx) * TCX;
+        t /= tx;
+        y0 = (int)(t % ty) * TCY;
+        t /= ty;
+        z0 = (int)(t % tz) * TCZ;
+        box = (int)(t / tz);
+    };
+    const long long mine = (ntiles - (long long)blockIdx.x + gridDim.x - 1) / gridDim.x;  // tiles of this CTA
+    long long issued = 0;  // tiles whose MMAs the MMA warp committed
+
+    if (warp < kTc2Load) {
+        // ---- loaders: halo tiles into the ring, one stage of lag on the announcement
+        for (long long i = 0; i < mine; i++) {
+            const int sa = (int)(i % NA);
+            if (i >= NA && !mhd::mbar_wait_bounded(&a_empty[sa], (uint32_t)(((i / NA) - 1) & 1), err))
+                break;
+            int b_, z_, y_, x_;
+            coords((long long)blockIdx.x + i * gridDim.x, b_, z_, y_, x_);
+            tc_load_halo<CIN>(sm + sa * ABYTES, x, b_, z_, y_, x_, n, tid, LOADERS);  // one commit group
+            if (i >= 1) {  // the previous tile's copies have landed: announce it
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive1(&a_full[(int)((i - 1) % NA)]);
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (mine > 0)
+            mbar_arrive1(&a_full[(int)((mine - 1) % NA)]);
+    } else if (warp == MMA_WARP) {
+        // ---- MMA issuer
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | (8u << 24);
+        const uint64_t b_desc = umma_desc(mhd::smem_u32(sW), COUT * 16, 128);
+        for (long long i = 0; i < mine; i++) {
+            const int sa = (int)(i % NA), st = (int)(i % NT);
+            if (!mhd::mbar_wait_bounded(&a_full[sa], (uint32_t)((i / NA) & 1), err))
+                break;
+            if (i >= NT && !mhd::mbar_wait_bounded(&t_empty[st], (uint32_t)(((i / NT) - 1) & 1), err))
+                break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (lane == 0) {
+                tc_issue_tile<CIN, COUT>(tmem + 64 * st, umma_desc(mhd::smem_u32(sm + sa * ABYTES), kChunkBytes, HY * 16),
+                                         b_desc, idesc);
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 mhd::smem_u32(&a_empty[sa]))
+                             : "memory");
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 mhd::smem_u32(&t_full[st]))
+                             : "memory");
+            }
+            __syncwarp();
+            issued = i + 1;
+        }
+        // the last committed MMAs have completed before TMEM is freed
+        if (issued > 0)
+            mhd::mbar_wait_bounded(&t_full[(int)((issued - 1) % NT)], (uint32_t)(((issued - 1) / NT) & 1), err);
+    } else {
+        // ---- epilogue: lanes 32 (warp % 4).. of both planes
+        const int q = warp & 3;
+        for (long long i = 0; i < mine; i++) {
+            const int st = (int)(i % NT);
+            if (!mhd::mbar_wait_bounded(&t_full[st], (uint32_t)((i / NT) & 1), err))
+                break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            uint32_t r0[32], r1[32];
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + 64 * st, r0);
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + 64 * st + 32, r1);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive1(&t_empty[st]);
+            int box, z0, y0, x0;
+            coords((long long)blockIdx.x + i * gridDim.x, box, z0, y0, x0);
+            const int m = q * 32 + lane, vx = m >> 3, vy = m & 7;
+            const size_t v = (((size_t)box * n + z0) * n + (y0 + vy)) * n + (x0 + vx);
+            tc_epilogue_row<COUT, EPI>(r0, v, bias, y, zsave, zprev);
+            tc_epilogue_row<COUT, EPI>(r1, v + (size_t)n * n, bias, y, zsave, zprev);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == MMA_WARP)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
 }
 
 // dW(co, tap, ci) = sum_v dz(v, co) a(v + off(tap), ci).  Warp w owns the taps
@@ -1025,11 +1214,37 @@ int launch_conv(const void* x, const void* w, const float* bias, void* y, void* 
 
 int* g_tc_err = nullptr;  // device error word of the tcgen05 kernels
 bool g_tc_disabled = false;
+bool g_tc_two_buffer = false;  // the single-loop two-buffer kernel in place of the warp-specialised one
+
+template <int CIN, int COUT, int EPI>
+int launch_conv_tc2(const void* x, const void* w, const float* bias, void* y, void* zsave, const void* zprev, int nb,
+                    int n, cudaStream_t s)
+{
+    constexpr size_t smem = tc2_smem_bytes<CIN, COUT>();
+    static bool attr = false;
+    if (!attr) {
+        if (set_smem(k_conv_tc2<CIN, COUT, EPI>, smem) != cudaSuccess)
+            return MHD_ERR_CUDA;
+        attr = true;
+    }
+    const long long ntiles = (long long)nb * (n / TCX) * (n / TCY) * (n / TCZ);
+    const long long grid = ntiles < (long long)sms() ? ntiles : (long long)sms();
+    k_conv_tc2<CIN, COUT, EPI><<<(unsigned)grid, kTc2Warps * 32, smem, s>>>(
+        static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias, y, static_cast<bf16*>(zsave),
+        static_cast<const bf16*>(zprev), n, ntiles, g_tc_err);
+    return st(cudaGetLastError());
+}
 
 template <int CIN, int COUT, int EPI>
 int launch_conv_tc(const void* x, const void* w, const float* bias, void* y, void* zsave, const void* zprev, int nb,
                    int n, cudaStream_t s)
 {
+    if (!g_tc_err && cudaMalloc(&g_tc_err, sizeof(int)) == cudaSuccess)
+        cudaMemset(g_tc_err, 0, sizeof(int));
+    if (!g_tc_err)
+        return MHD_ERR_NOMEM;
+    if (!g_tc_two_buffer)
+        return launch_conv_tc2<CIN, COUT, EPI>(x, w, bias, y, zsave, zprev, nb, n, s);
     const size_t smem = 2 * (size_t)(CIN / 8) * kChunkBytes + (size_t)27 * (CIN / 8) * COUT * 16;  // A x 2, W
     static bool attr = false;
     if (!attr) {
@@ -1132,8 +1347,9 @@ extern "C" MHD_API int mhd_cl_conv(int kind, const void* x, const void* w, const
 // mma.sync kernels everywhere.  Returns the previous setting.
 extern "C" MHD_API int mhd_cl_use_tcgen05(int enable)
 {
-    const int prev = g_tc_disabled ? 0 : 1;
+    const int prev = g_tc_disabled ? 0 : (g_tc_two_buffer ? 2 : 1);
     g_tc_disabled = (enable == 0);
+    g_tc_two_buffer = (enable == 2);
     return prev;
 }
 

@@ -38,8 +38,10 @@ extern "C" {
 MHD_API int mhd_cl_conv(int kind, const void *x, const void *w, const float *bias, void *y, void *zsave,
                         const void *zprev, int nb, int n, void *stream);
 /* The 3^3 kinds (FWD_IN, FWD_HID, DGRAD_HID) run on tcgen05 (TMEM accumulators) when n is a multiple
- * of 16, on mma.sync otherwise; mhd_cl_use_tcgen05(0) forces mma.sync everywhere (returns the previous
- * setting).  mhd_cl_device_errors returns (and clears) the tcgen05 kernels' timeout bits. */
+ * of 16, on mma.sync otherwise; mhd_cl_use_tcgen05(0) forces mma.sync everywhere, (1) selects the
+ * warp-specialised tcgen05 kernel (the default), (2) the two-buffer tcgen05 kernel with one loop for
+ * all warps (returns the previous setting).  mhd_cl_device_errors returns (and clears) the tcgen05
+ * kernels' timeout bits. */
 MHD_API int mhd_cl_use_tcgen05(int enable);
 MHD_API int mhd_cl_device_errors(void);
 /* bytes of FP32 scratch that mhd_cl_wgrad needs (-1 for a bad argument) */

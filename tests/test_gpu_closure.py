@@ -272,7 +272,7 @@ def test_tcgen05_conv_matches_mma_sync(kind, clos, cuda):
     bd = to_f32(torch, rng.normal(size=32) * 0.1)
     zp = to_bf16(torch, rng.normal(size=(nb, n, n, n, 32)))
     outs = []
-    for tc in (1, 0):
+    for tc in (1, 0, 2):  # warp-specialised tcgen05, mma.sync, two-buffer tcgen05
         L.mhd_cl_use_tcgen05(tc)
         y = torch.empty(nb * n ** 3 * 32, dtype=torch.bfloat16, device="cuda")
         z = torch.zeros_like(y)
@@ -290,3 +290,7 @@ def test_tcgen05_conv_matches_mma_sync(kind, clos, cuda):
     assert rel(outs[0][0], outs[1][0]) < 8e-3  # FP32 accumulation in two orders, one BF16 rounding
     if kind != "dgrad":
         assert rel(outs[0][1], outs[1][1]) < 8e-3
+    # the two tcgen05 kernels issue the same MMAs in the same order: the same bits
+    assert np.array_equal(outs[0][0], outs[2][0])
+    if kind != "dgrad":
+        assert np.array_equal(outs[0][1], outs[2][1])
