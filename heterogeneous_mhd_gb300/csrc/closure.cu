@@ -369,6 +369,60 @@ __device__ __forceinline__ void tc_epilogue_row(const uint32_t (&r)[32], size_t 
     }
 }
 
+// The same epilogue with GELU and GELU' read from tables indexed by the BF16
+// bits of the pre-activation (gelu_tab: the BF16 bits of gelu, grad_tab: the
+// FP32 gelu'), which hold exactly what gelu() and gelu_grad() give on those
+// 65536 inputs: the results are the computed epilogue's bit for bit.
+template <int COUT, int EPI>
+__device__ __forceinline__ void tc_epilogue_row_tab(const uint32_t (&r)[32], size_t v, const float* __restrict__ bias,
+                                                    void* __restrict__ y, bf16* __restrict__ zsave,
+                                                    const bf16* __restrict__ zprev,
+                                                    const unsigned short* __restrict__ gelu_tab,
+                                                    const float* __restrict__ grad_tab)
+{
+    __align__(16) bf16 o1[COUT];
+    __align__(16) bf16 o2[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; c += 2) {
+        const float v0 = __uint_as_float(r[c]), v1 = __uint_as_float(r[c + 1]);
+        if constexpr (EPI == EPI_GELU) {
+            const __nv_bfloat162 zz = __floats2bfloat162_rn(v0 + bias[c], v1 + bias[c + 1]);
+            *reinterpret_cast<__nv_bfloat162*>(o2 + c) = zz;
+            const uint32_t bits = *reinterpret_cast<const uint32_t*>(&zz);
+            const uint32_t g = (uint32_t)__ldg(gelu_tab + (bits & 0xFFFFu)) |
+                               ((uint32_t)__ldg(gelu_tab + (bits >> 16)) << 16);
+            *reinterpret_cast<uint32_t*>(o1 + c) = g;
+        } else {
+            const uint32_t zb = *reinterpret_cast<const uint32_t*>(zprev + v * COUT + c);
+            *reinterpret_cast<__nv_bfloat162*>(o1 + c) =
+                __floats2bfloat162_rn(v0 * __ldg(grad_tab + (zb & 0xFFFFu)), v1 * __ldg(grad_tab + (zb >> 16)));
+        }
+    }
+    uint4* yo = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + v * COUT);
+#pragma unroll
+    for (int k = 0; k < COUT / 8; k++)
+        yo[k] = reinterpret_cast<const uint4*>(o1)[k];
+    if constexpr (EPI == EPI_GELU) {
+        uint4* zo = reinterpret_cast<uint4*>(zsave + v * COUT);
+#pragma unroll
+        for (int k = 0; k < COUT / 8; k++)
+            zo[k] = reinterpret_cast<const uint4*>(o2)[k];
+    }
+}
+
+// gelu and gelu' of every BF16 value (the tables of tc_epilogue_row_tab)
+__global__ void k_gelu_tables(unsigned short* __restrict__ gelu_tab, float* __restrict__ grad_tab)
+{
+    const int code = blockIdx.x * blockDim.x + threadIdx.x;
+    if (code >= 65536)
+        return;
+    const unsigned short b = (unsigned short)code;
+    const float z = __bfloat162float(*reinterpret_cast<const bf16*>(&b));
+    const bf16 g = __float2bfloat16_rn(gelu(z));
+    gelu_tab[code] = *reinterpret_cast<const unsigned short*>(&g);
+    grad_tab[code] = gelu_grad(z);
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
 {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
@@ -541,7 +595,7 @@ template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(kTc2Warps * 32, 1)
     k_conv_tc2(const bf16* __restrict__ x, const bf16* __restrict__ w, const float* __restrict__ bias,
                void* __restrict__ y, bf16* __restrict__ zsave, const bf16* __restrict__ zprev, int n, long long ntiles,
-               int* err)
+               int* err, const unsigned short* __restrict__ gelu_tab, const float* __restrict__ grad_tab)
 {
     static_assert(COUT == 32, "one tile's accumulators are 2 x 32 TMEM columns");
     constexpr int CH = CIN / 8, NA = tc2_stages<CIN>(), NT = kTc2NT;
@@ -659,8 +713,8 @@ __global__ void __launch_bounds__(kTc2Warps * 32, 1)
             coords((long long)blockIdx.x + i * gridDim.x, box, z0, y0, x0);
             const int m = q * 32 + lane, vx = m >> 3, vy = m & 7;
             const size_t v = (((size_t)box * n + z0) * n + (y0 + vy)) * n + (x0 + vx);
-            tc_epilogue_row<COUT, EPI>(r0, v, bias, y, zsave, zprev);
-            tc_epilogue_row<COUT, EPI>(r1, v + (size_t)n * n, bias, y, zsave, zprev);
+            tc_epilogue_row_tab<COUT, EPI>(r0, v, bias, y, zsave, zprev, gelu_tab, grad_tab);
+            tc_epilogue_row_tab<COUT, EPI>(r1, v + (size_t)n * n, bias, y, zsave, zprev, gelu_tab, grad_tab);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1216,11 +1270,30 @@ int* g_tc_err = nullptr;  // device error word of the tcgen05 kernels
 bool g_tc_disabled = false;
 bool g_tc_two_buffer = false;  // the single-loop two-buffer kernel in place of the warp-specialised one
 
+unsigned short* g_gelu_tab = nullptr;  // gelu / gelu' tables of the warp-specialised convolution
+float* g_grad_tab = nullptr;
+
 template <int CIN, int COUT, int EPI>
 int launch_conv_tc2(const void* x, const void* w, const float* bias, void* y, void* zsave, const void* zprev, int nb,
                     int n, cudaStream_t s)
 {
     constexpr size_t smem = tc2_smem_bytes<CIN, COUT>();
+    if (!g_gelu_tab) {  // once per process, ordered before the first use on this stream
+        unsigned short* gt = nullptr;
+        float* dt = nullptr;
+        if (cudaMalloc(&gt, 65536 * sizeof(unsigned short)) != cudaSuccess ||
+            cudaMalloc(&dt, 65536 * sizeof(float)) != cudaSuccess) {
+            cudaFree(gt);
+            return MHD_ERR_NOMEM;
+        }
+        k_gelu_tables<<<256, 256, 0, s>>>(gt, dt);
+        // complete before any stream uses them (the first convolution is never captured:
+        // a corrected step runs once uncaptured before its graph is built)
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+            return MHD_ERR_CUDA;
+        g_gelu_tab = gt;
+        g_grad_tab = dt;
+    }
     static bool attr = false;
     if (!attr) {
         if (set_smem(k_conv_tc2<CIN, COUT, EPI>, smem) != cudaSuccess)
@@ -1231,7 +1304,7 @@ int launch_conv_tc2(const void* x, const void* w, const float* bias, void* y, vo
     const long long grid = ntiles < (long long)sms() ? ntiles : (long long)sms();
     k_conv_tc2<CIN, COUT, EPI><<<(unsigned)grid, kTc2Warps * 32, smem, s>>>(
         static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias, y, static_cast<bf16*>(zsave),
-        static_cast<const bf16*>(zprev), n, ntiles, g_tc_err);
+        static_cast<const bf16*>(zprev), n, ntiles, g_tc_err, g_gelu_tab, g_grad_tab);
     return st(cudaGetLastError());
 }
 

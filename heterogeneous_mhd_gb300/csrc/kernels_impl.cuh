@@ -100,9 +100,10 @@ static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
     size_t smem = fluidx2_smem_elems(C * T, a.P) * sizeof(R);
     if constexpr (AX != 0) {
         // the x-major state as (5 nx words, ny, nz) for u and (3 nx, ny, nz) for b;
-        // boxes of P cells along x by the whole pencil along y (AX 1) or z (AX 2)
-        constexpr int n = C * T;
-        const uint32_t by = (AX == 1) ? n : 1, bz = (AX == 1) ? 1 : n;
+        // boxes of P cells along x by the pencil along y (AX 1) or z (AX 2), in
+        // boxes of at most 256 rows
+        constexpr int n = C * T, rows = (n + 255) / 256 > 1 ? n / ((n + 255) / 256) : n;
+        const uint32_t by = (AX == 1) ? rows : 1, bz = (AX == 1) ? 1 : rows;
         const uint64_t ny = a.ny, nz = a.nz;
         e = encode_map_3d(&tm.u_in, a.uu, 5ull * a.nx, ny, nz, 5 * kSweepP, by, bz);
         if (e == cudaSuccess)
@@ -122,13 +123,13 @@ static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
 }
 
 // Sweep of the untransposed state along y or z (fused step, FP32): pencils
-// of n = 4T <= 256 cells along the sweep (one tensor box), four pencils at
-// consecutive x per CTA (nx a multiple of 4, so every box starts on a
-// 16-byte boundary), one box of the state.
+// of n = 4T <= 512 cells along the sweep (one or two tensor boxes), four
+// pencils at consecutive x per CTA (nx a multiple of 4, so every box starts
+// on a 16-byte boundary), one box of the state.
 static bool plan_fluidx_sweep(int n, int nx, int nbox, FxPlan& p)
 {
     p = FxPlan{0, 0, 0};
-    if (!kV2 || nbox != 1 || n % 4 != 0 || !pow2_in(n / 4, 8, 64) || nx % kSweepP != 0)
+    if (!kV2 || nbox != 1 || n % 4 != 0 || !pow2_in(n / 4, 8, 128) || nx % kSweepP != 0)
         return false;
     p.C = 4, p.T = n / 4, p.P = kSweepP;
     return true;
@@ -144,6 +145,7 @@ static cudaError_t fluidx_sweep(FluidxArgs a, const FxPlan& p, cudaStream_t s)
         case 16: return launch_fx2<4, 16, AX>(a, s);
         case 32: return launch_fx2<4, 32, AX>(a, s);
         case 64: return launch_fx2<4, 64, AX>(a, s);
+        case 128: return launch_fx2<4, 128, AX>(a, s);
         }
     }
     return cudaErrorInvalidValue;

@@ -1,6 +1,6 @@
 // Batched boxes: many independent periodic cubes of uneven sizes advanced
-// together, each with its own dt (config 3 of the project: 256 boxes of edge
-// 32..128).
+// together, each with its own dt (the benchmarked workload: 256 boxes of
+// edge 32..128).
 //
 // The boxes are grouped by edge length.  Each size class keeps its boxes'
 // states contiguous (ping-pong pairs like the single-box context), so every

@@ -72,9 +72,12 @@ __host__ __device__ inline size_t fluidx_sweep_smem_bytes(int n)
 }
 
 template <typename R, bool EX, int C, int T, int AX = 0>
-__global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const __grid_constant__ SweepMaps tm)
+__global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1) : 0)
+    k_fluidx2(FluidxArgs a, const __grid_constant__ SweepMaps tm)
 {
-    static_assert(AX == 0 || (sizeof(R) == 4 && C == 4 && T <= 64), "sweeps along y, z: FP32, 4 cells, n <= 256");
+    static_assert(AX == 0 || (sizeof(R) == 4 && C == 4 && T <= 128), "sweeps along y, z: FP32, 4 cells, n <= 512");
+    // y/z sweeps: a tensor box holds at most 256 rows, so longer pencils move in NBX boxes of BXR rows
+    constexpr int NBX = (C * T + 255) / 256, BXR = C * T / NBX;
     select_box(a, blockIdx.z, sizeof(CflPart<R>));
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -141,10 +144,14 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const
             // coordinates (x word, y, z): the pencil runs along y (AX 1) or z (AX 2) from 0
             const int y = (AX == 1) ? 0 : kk, z = (AX == 1) ? kk : 0;
             const int yk = (AX == 1) ? 0 : kn, zk = (AX == 1) ? kn : 0;
-            tma_load_3d(rows_u, &tm.u_in, 5 * x0, y, z, &bar);
-            tma_load_3d(rows_b, &tm.b_in, 3 * x0, y, z, &bar);
-            tma_load_3d(rows_bk, &tm.b_in, 3 * x0, yk, zk, &bar);
-            tma_load_3d(rows_bn, &tm.bn_in, 3 * xn, y, z, &bar);
+#pragma unroll
+            for (int h = 0; h < NBX; h++) {  // rows h*BXR.. of the pencil
+                const int dy = (AX == 1) ? h * BXR : 0, dz = (AX == 1) ? 0 : h * BXR;
+                tma_load_3d(rows_u + h * BXR * 5 * kSweepP, &tm.u_in, 5 * x0, y + dy, z + dz, &bar);
+                tma_load_3d(rows_b + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, y + dy, z + dz, &bar);
+                tma_load_3d(rows_bk + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, yk + dy, zk + dz, &bar);
+                tma_load_3d(rows_bn + h * BXR * 4, &tm.bn_in, 3 * xn, y + dy, z + dz, &bar);
+            }
         }
         __syncthreads();
         if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
@@ -484,9 +491,13 @@ __global__ void __launch_bounds__(256, AX ? 3 : 0) k_fluidx2(FluidxArgs a, const
         __syncthreads();
         if (tid == 0) {
             const int x0 = blockIdx.x * P, kk = blockIdx.y;
-            tma_store_3d(&tm.u_out, 5 * x0, (AX == 1) ? 0 : kk, (AX == 1) ? kk : 0, rows_u);
-            if (wc)
-                tma_store_3d(&tm.w_out, 2 * x0, (AX == 1) ? 0 : kk, (AX == 1) ? kk : 0, rows_w);
+#pragma unroll
+            for (int h = 0; h < NBX; h++) {
+                const int py = (AX == 1) ? h * BXR : kk, pz = (AX == 1) ? kk : h * BXR;
+                tma_store_3d(&tm.u_out, 5 * x0, py, pz, rows_u + h * BXR * 5 * kSweepP);
+                if (wc)
+                    tma_store_3d(&tm.w_out, 2 * x0, py, pz, rows_w + h * BXR * 2 * kSweepP);
+            }
             tma_store_commit();
             tma_store_wait_all();
         }

@@ -26,7 +26,7 @@ from pathlib import Path
 DEFAULTS = {
     "n": 64,              # cube edge (nx = ny = nz unless given)
     "nx": 0, "ny": 0, "nz": 0,
-    "ic": "vortex",       # vortex (config 1) or turbulence (config 2)
+    "ic": "vortex",       # vortex (64^3 Orszag-Tang-like vortex) or turbulence (decaying turbulence)
     "seed": 0,
     "steps": 100,
     "cfl": 0.7,

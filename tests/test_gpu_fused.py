@@ -95,3 +95,21 @@ def test_fused_sweep_kernels_exact_vs_oracle(shape, knobs, mhd, cuda, oracle32):
         autotune.apply({k: 0 for k in knobs})
     assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1]), (shape, knobs)
     assert np.float32(t) == np.float32(ref[2])
+
+
+def test_fused_sweeps_of_512_cells_exact_vs_oracle(mhd, cuda):
+    """Pencils of 512 cells along y and z: the fluidx sweep moves each CTA's
+    rows in two tensor boxes of 256 and runs four 128-thread pencils; EXACT
+    fused steps bit for bit against the oracle of the reference's C path and
+    against the plain step.  The reference's loop transposes x with z, so its
+    boxes have ny == nz."""
+    from _oracle import Oracle
+    oracle32 = Oracle(32, "port")
+    shape = (32, 512, 512)
+    u0, b0 = mhd.init_vortex(*shape, seed=6, vscale=1.2)
+    ref = oracle32.strang(u0, b0, *shape, 2)
+    u, b, t = run(mhd, u0, b0, shape, 2, fused=True, exact=True)
+    assert bitwise_equal(u, ref[0]) and bitwise_equal(b, ref[1]), shape
+    assert np.float32(t) == np.float32(ref[2])
+    up, bp, tp = run(mhd, u0, b0, shape, 2, fused=False, exact=True)
+    assert bitwise_equal(u, up) and bitwise_equal(b, bp) and t == tp

@@ -62,7 +62,7 @@ def test_exact_steps_bitwise_vs_reference_golden(bits, mhd, cuda):
 
 
 def test_exact_64_vortex_checksums_fp32(mhd, cuda):
-    """Config 1 (64^3, CFL 0.7): the reference's state hash after 1, 10, 100 steps."""
+    """The 64^3 vortex (CFL 0.7): the reference's state hash after 1, 10, 100 steps."""
     ck = checksums()["f32"]
     u0, b0 = mhd.init_vortex(64, 64, 64, seed=0)
     assert sha(u0, b0) == ck["init"]
@@ -93,7 +93,7 @@ def test_exact_64_vortex_checksums_fp64(mhd, cuda):
 
 
 def test_fast_64_vortex_tolerance(mhd, cuda, oracle32, oracle64):
-    """Config 1 with the production kernels: per-field relative L2 against the
+    """The 64^3 vortex with the production kernels: per-field relative L2 against the
     reference C after 1 and 100 steps, and the FP32-vs-FP64 error of both."""
     u0, b0 = mhd.init_vortex(64, 64, 64, seed=0)
     s = (64, 64, 64)
@@ -155,7 +155,7 @@ def test_tf_clamp_and_time(mhd, cuda, oracle32):
 
 
 def test_full_size_256_turbulence_vs_oracle(mhd, cuda, oracle32):
-    """Config 2 at full size (256^3): one step of the production kernels
+    """The decaying-turbulence box at full size (256^3): one step of the production kernels
     against the reference C (oracle), and the EXACT kernels bit for bit."""
     n = 256
     u0, b0 = mhd.init_turbulence(n, seed=0)
@@ -170,7 +170,7 @@ def test_full_size_256_turbulence_vs_oracle(mhd, cuda, oracle32):
 
 @pytest.mark.slow
 def test_full_size_256_turbulence_100_steps_vs_oracle(mhd, cuda, oracle32):
-    """Config 2 at 256^3 after 100 steps: the EXACT kernels bit for bit with
+    """The decaying-turbulence box at 256^3 after 100 steps: the EXACT kernels bit for bit with
     the reference C (oracle), and the production kernels within FAST_256_100_TOL
     per field (the error is recorded).  The oracle runs on all host cores
     (about three minutes)."""
