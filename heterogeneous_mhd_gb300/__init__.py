@@ -91,6 +91,7 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
         "mhd_state_ptrs": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
         "mhd_clock_ptr": (C.c_int, [_vp, C.POINTER(_vp)]),
         "mhd_step": (C.c_int, [_vp, C.c_int, C.c_double, C.c_int]),
+        "mhd_step_host": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_double, C.c_int]),
         "mhd_set_time": (C.c_int, [_vp, C.c_double, C.c_double]),
         "mhd_get_time": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                    C.POINTER(C.c_longlong)]),
@@ -294,6 +295,19 @@ class Context:
 
     def step(self, nsteps: int = 1, cfl: float = 0.7, fused: bool = False) -> None:
         _check(lib().mhd_step(self._h, nsteps, cfl, MHD_FUSED if fused else MHD_PLAIN), "mhd_step")
+
+    def step_host(self, u, b, nsteps: int = 1, cfl: float = 0.7, fused: bool = False) -> None:
+        """nsteps steps on a host state: u and b (contiguous host arrays of the
+        context's dtype, e.g. pinned tensors) are copied in, stepped and
+        overwritten with the result (mhd_step_host)."""
+        n = self.nx * self.ny * self.nz
+        for a, k in ((u, 5), (b, 3)):
+            if self._where(a) != MHD_HOST:
+                raise ValueError("step_host takes host arrays")
+            if isinstance(a, np.ndarray) and (not a.flags.c_contiguous or a.dtype != self.dtype or a.size != k * n):
+                raise ValueError(f"step_host wants contiguous {self.dtype.__name__} arrays of {k} * nx*ny*nz")
+        _check(lib().mhd_step_host(self._h, _ptr(u), _ptr(b), nsteps, cfl, MHD_FUSED if fused else MHD_PLAIN),
+               "mhd_step_host")
 
     def set_time(self, t: float = 0.0, tf: float = float("inf")) -> None:
         _check(lib().mhd_set_time(self._h, t, tf), "mhd_set_time")

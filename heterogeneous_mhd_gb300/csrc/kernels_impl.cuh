@@ -93,8 +93,8 @@ static cudaError_t launch_fx2(const FluidxArgs& a, cudaStream_t s)
     cudaError_t e = allow_smem(k_fluidx2<R, EX, C, T, AX>, attr, true);
     if (e != cudaSuccess)
         return e;
-    // grid: (pencil groups along j, planes along k, boxes)
-    const int nj = (AX == 0) ? a.ny : a.nx, nk = (AX == 2) ? a.ny : a.nz;
+    // grid: (pencil groups along j, planes along k (a range along z: kcount), boxes)
+    const int nj = (AX == 0) ? a.ny : a.nx, nk = (AX == 2) ? a.ny : (a.kcount ? a.kcount : a.nz);
     dim3 grid(nj / a.P, nk, a.bs.count);
     SweepMaps tm{};
     size_t smem = fluidx2_smem_elems(C * T, a.P) * sizeof(R);
@@ -151,9 +151,22 @@ static cudaError_t fluidx_sweep(FluidxArgs a, const FxPlan& p, cudaStream_t s)
     return cudaErrorInvalidValue;
 }
 
+// A plane range (kcount) is taken by the x sweep's and the y sweep's
+// register-engine kernels (k_fluidx2) of one box, nowhere else.
+static bool fluidx_range_ok(const FluidxArgs& a)
+{
+    if (a.kcount == 0 && a.kbeg == 0)
+        return true;
+    if (a.kcount <= 0 || a.kbeg < 0 || a.kbeg + a.kcount > a.nz || a.axis == 2 || a.bs.count != 1)
+        return false;
+    return a.axis == 1 || plan_fluidx(a.nx, a.ny, a.use_tma != 0).C != 0;
+}
+
 static cudaError_t fluidx(const FluidxArgs& in, cudaStream_t s)
 {
     FluidxArgs a = in;
+    if (!fluidx_range_ok(a))
+        return cudaErrorInvalidValue;
     if (a.axis != 0) {
         FxPlan p;
         const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.uu) |
@@ -466,7 +479,7 @@ static cudaError_t launch_ad6(const AdvectArgs& a, int K, cudaStream_t s)
         if (e != cudaSuccess)
             return e;
     }
-    dim3 grid(a.ny / J, a.nz / K, a.bs.count);
+    dim3 grid(a.ny / J, (a.kcount ? a.kcount : a.nz) / K, a.bs.count);
     k_advect6<EX, C, J, SW><<<grid, advect6_threads(J), advect6_smem_bytes(C * 32, J), s>>>(b, wmap);
     return cudaGetLastError();
 }
@@ -583,6 +596,15 @@ static cudaError_t launch_ad2(const AdvectArgs& a, cudaStream_t s)
 static cudaError_t advect(const AdvectArgs& in, cudaStream_t s)
 {
     AdvectArgs a = in;
+    if (a.kcount != 0 || a.kbeg != 0) {  // a plane range: the warp-per-pencil x-sweep kernel only
+        const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
+                             reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub);
+        A6Plan p6;
+        if (a.kcount <= 0 || a.kbeg < 0 || a.kbeg + a.kcount > a.nz || !plan_advect6(a, (al & 15) == 0, p6) ||
+            a.kcount % p6.K != 0 || a.kbeg % p6.K != 0)
+            return cudaErrorInvalidValue;
+        return advect_x6(a, p6, s);
+    }
     if (a.axis != 0) {  // fused step: pencils along y or z of the untransposed state
         if constexpr (kV2) {
             A4Plan p5;
@@ -691,13 +713,13 @@ static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
 
 // ------------------------------------------------------------------ calcfl
 
-static cudaError_t calcfl(const void* u, const void* b, size_t ncell, void* part, int* nparts, const BoxStrides& bs,
-                          cudaStream_t s)
+static cudaError_t calcfl(const void* u, const void* b, size_t ncell, size_t cell0, void* part, int* nparts,
+                          const BoxStrides& bs, cudaStream_t s)
 {
     const int blocks = (int)((ncell + 255) / 256);
     *nparts = blocks;
     k_calcfl<R, EX><<<dim3(blocks, bs.count), 256, 0, s>>>(static_cast<const R*>(u), static_cast<const R*>(b), ncell,
-                                                           static_cast<CflPart<R>*>(part), bs);
+                                                           cell0, static_cast<CflPart<R>*>(part), bs);
     return cudaGetLastError();
 }
 
@@ -767,9 +789,27 @@ static int sweep_writes_w(int axis, int nx, int ny, int nz)
     return kV2 && (axis == 1 || axis == 2) && plan_fluidx_sweep(axis == 1 ? ny : nz, nx, 1, p);
 }
 
+static int tail_slabs_ok(int nx, int ny, int nz, int kcount)
+{
+    if (!kV2 || kcount <= 0 || nz % kcount != 0 || !sweep_writes_w(1, nx, ny, nz))
+        return 0;
+    FxPlan p;
+    const bool aligned = ((size_t)nx * 5 * sizeof(R)) % 16 == 0 && ((size_t)nx * 3 * sizeof(R)) % 16 == 0;
+    if (!plan_fluidx_sweep(ny, nx, 1, p) || plan_fluidx(nx, ny, aligned).C == 0)
+        return 0;
+    // the x-sweep advectbyzx with a side array (any 16-byte aligned address stands in for the buffers)
+    AdvectArgs a{};
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.ub = a.b1_src = a.w = reinterpret_cast<const void*>(uintptr_t(256));
+    A6Plan p6;
+    return (plan_advect6(a, aligned, p6) && kcount % p6.K == 0) ? 1 : 0;
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
                                sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w, transpose_writes_w,
-                               sweep_writes_w};
+                               sweep_writes_w, tail_slabs_ok};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

@@ -118,6 +118,15 @@ struct mhd_ctx {
                         // transposes write it, every advectbyzx reads it
     int* err_dev = nullptr;
     long long* nsteps_dev = nullptr;
+    // host-buffer steps (mhd_step_host): the copy stream, its events, and the
+    // host arrays the last step's result goes to (set only while that step is
+    // enqueued; the step copies b out after its last advectbyzx, u after its
+    // last fluidx)
+    cudaStream_t cstream = nullptr;
+    std::vector<cudaEvent_t> cev;
+    void* out_u = nullptr;
+    void* out_b = nullptr;
+    int slab_beg = 0, slab_count = 0;  // plane range along z of the next operators (0 planes: all)
     bool have_state = false;
     bool cfl_valid = false;  // part holds the CFL partials of the current state
     int cfl_nparts = 0;
@@ -285,6 +294,12 @@ extern "C" MHD_API int mhd_destroy(mhd_ctx* c)
     invalidate_graphs(c);
     for (auto& e : c->ev_free)
         cudaEventDestroy(e);
+    if (c->cstream) {
+        cudaStreamSynchronize(c->cstream);
+        cudaStreamDestroy(c->cstream);
+    }
+    for (auto& e : c->cev)
+        cudaEventDestroy(e);
     for (int v = 0; v < 2; v++) {
         c->U[v].release();
         c->B[v].release();
@@ -340,6 +355,8 @@ static int op_fluidx(mhd_ctx* c, void* u, const void* uu, const void* ub, int nx
     a.axis = axis;
     a.w_out = w_out;
     a.w_comp = w_comp;
+    a.kbeg = c->slab_beg;
+    a.kcount = c->slab_count;
     KTimer kt(c, MHD_K_FLUIDX);
     CUDA_TRY(c->ks->fluidx(a, c->stream));
     return MHD_OK;
@@ -363,6 +380,8 @@ static int op_advect(mhd_ctx* c, void* b_out, const void* b1_src, const void* uu
     a.err = c->err_dev;
     a.axis = axis;
     a.w = w;
+    a.kbeg = c->slab_beg;
+    a.kcount = c->slab_count;
     KTimer kt(c, MHD_K_ADVECT);
     CUDA_TRY(c->ks->advect(a, c->stream));
     return MHD_OK;
@@ -399,7 +418,7 @@ static int op_calcfl_partials(mhd_ctx* c, DevBuf& dst, const void* u, const void
 {
     MHD_TRY(dst.ensure(((cells + 255) / 256 + 1) * c->ks->part_bytes));
     KTimer kt(c, MHD_K_CALCFL);
-    CUDA_TRY(c->ks->calcfl(u, b, cells, dst.p, np, BoxStrides{}, c->stream));
+    CUDA_TRY(c->ks->calcfl(u, b, cells, 0, dst.p, np, BoxStrides{}, c->stream));
     return MHD_OK;
 }
 
@@ -544,25 +563,31 @@ extern "C" MHD_API int mhd_op_calcfl(mhd_ctx* c, const void* u, const void* b, i
 
 // ----------------------------------------------------------------- state
 
+// The state's device buffers, allocated once: the ping-pong state, the CFL
+// partials of both producers (the first CFL pass and the fluidx epilogue)
+// and the side array, so that a captured step never allocates.
+static int ensure_state(mhd_ctx* c)
+{
+    const size_t bu = ncell(c) * 5 * c->elem, bb = ncell(c) * 3 * c->elem;
+    for (int v = 0; v < 2; v++) {
+        MHD_TRY(c->U[v].ensure(bu));
+        MHD_TRY(c->B[v].ensure(bb));
+    }
+    MHD_TRY(c->cflred.ensure((size_t)kCflReduceCtas * c->ks->part_bytes));
+    if (c->elem == 4)  // the side array of the plain and fused steps
+        MHD_TRY(c->W.ensure(ncell(c) * 2 * sizeof(float)));
+    const size_t a = (ncell(c) + 255) / 256;
+    const size_t f = fluidx_parts(c);
+    MHD_TRY(c->part.ensure(((a > f ? a : f) + 1) * c->ks->part_bytes));
+    return MHD_OK;
+}
+
 extern "C" MHD_API int mhd_set_state(mhd_ctx* c, const void* u, const void* b, int where)
 {
     if (!c || !u || !b)
         return set_err(MHD_ERR_ARG);
     const size_t bu = ncell(c) * 5 * c->elem, bb = ncell(c) * 3 * c->elem;
-    for (int v = 0; v < 2; v++) {
-        MHD_TRY(set_err(c->U[v].ensure(bu)));
-        MHD_TRY(set_err(c->B[v].ensure(bb)));
-    }
-    MHD_TRY(set_err(c->cflred.ensure((size_t)kCflReduceCtas * c->ks->part_bytes)));
-    if (c->elem == 4)  // the side array of the plain step (allocated here: captured steps never allocate)
-        MHD_TRY(set_err(c->W.ensure(ncell(c) * 2 * sizeof(float))));
-    // CFL partials for both producers (standalone calcfl and the fluidx
-    // epilogue), allocated here so a captured step never reallocates.
-    {
-        const size_t a = (ncell(c) + 255) / 256;
-        const size_t f = fluidx_parts(c);
-        MHD_TRY(set_err(c->part.ensure(((a > f ? a : f) + 1) * c->ks->part_bytes)));
-    }
+    MHD_TRY(set_err(ensure_state(c)));
     (void)where;  // direction inferred from the pointers (unified addressing)
     const cudaMemcpyKind kind = cudaMemcpyDefault;
     if (cudaMemcpyAsync(c->U[0].p, u, bu, kind, c->stream) != cudaSuccess ||
@@ -644,6 +669,54 @@ extern "C" MHD_API int mhd_get_time(mhd_ctx* c, double* t, double* dt, long long
 
 // ------------------------------------------------------------- the step
 
+// Events of the copy stream: entry (the compute stream's queued work), b out,
+// u out, done, then one per copy-in chunk.
+enum { kCevEntry = 0, kCevOutB, kCevOutU, kCevDone, kCevChunk0 };
+constexpr int kHostChunks = 8;  // copy-in chunks of a host-buffer step
+
+// The last step of a host-buffer step copies the final b out as soon as the
+// last advectbyzx has written it (field 1) and u after the last fluidx
+// (field 0), on the copy stream: the b copy overlaps the last fluidx, which
+// reads b but does not write it.  Planes k0 .. k0+nk-1 along z (nk 0: all).
+// Nothing happens for other steps.
+static int copy_out(mhd_ctx* c, int field, int k0 = 0, int nk = 0)
+{
+    void* dst = field ? c->out_b : c->out_u;
+    if (!dst || c->capturing)
+        return MHD_OK;
+    cudaEvent_t e = c->cev[field ? kCevOutB : kCevOutU];
+    CUDA_TRY(cudaEventRecord(e, c->stream));
+    CUDA_TRY(cudaStreamWaitEvent(c->cstream, e, 0));
+    const size_t per_plane = (size_t)c->nx * c->ny * (field ? 3 : 5) * c->elem;
+    const size_t off = (size_t)k0 * per_plane, bytes = (nk ? (size_t)nk : (size_t)c->nz) * per_plane;
+    const char* src = static_cast<const char*>(field ? c->B[0].p : c->U[0].p) + off;
+    CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(dst) + off, src, bytes, cudaMemcpyDefault, c->cstream));
+    return MHD_OK;
+}
+
+// Sets the plane range of the operators enqueued while it lives.
+struct SlabRange {
+    mhd_ctx* c;
+    SlabRange(mhd_ctx* ctx, int k0, int nk) : c(ctx)
+    {
+        c->slab_beg = k0;
+        c->slab_count = nk;
+    }
+    ~SlabRange() { c->slab_beg = c->slab_count = 0; }
+};
+
+// Slabs of the fused step's tail in a host-buffer step: 8 (or 4) ranges of
+// planes along z when the tail's kernels take them, else 1 (no slabs).
+static int host_tail_slabs(const mhd_ctx* c, const void* Wy)
+{
+    if (!c->out_u || c->capturing || !Wy || !c->ks->tail_slabs_ok)
+        return 1;
+    for (int s : {8, 4})
+        if (c->nz % s == 0 && c->ks->tail_slabs_ok(c->nx, c->ny, c->nz, c->nz / s))
+            return s;
+    return 1;
+}
+
 // One plain Strang step on (U0,B0) -> (U0,B0), C/mhd.c:62-118 with the
 // copy_matrix calls replaced by ping-pong buffers.  Requires cfl_valid (the
 // partials of the current state in c->part): the last fluidx of the step
@@ -688,11 +761,13 @@ static int enqueue_plain_step(mhd_ctx* c, double cfl)
     W = tside(1, ny, nx, nz);
     MHD_TRY(op_transpose(c, 1, U1, B1, U0, B0, ny, nx, nz, W));
     MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0, W));
+    MHD_TRY(copy_out(c, 1));
     // last fluidx with the calcfl epilogue for the next step
     const size_t nparts = fluidx_parts(c);
     if (c->part.cap < nparts * c->ks->part_bytes)  // sized by mhd_set_state
         return MHD_ERR_ARG;
     MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, c->part.p));
+    MHD_TRY(copy_out(c, 0));
     c->cfl_nparts = (int)nparts;
     return MHD_OK;
 }
@@ -728,13 +803,54 @@ static int enqueue_fused_step(mhd_ctx* c, double cfl)
     MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, nullptr, 2, Wz, 2));
     // y
     MHD_TRY(op_advect(c, B1, B0, U0, B0, nx, ny, nz, 0, dt, 1, Wz));
-    MHD_TRY(op_fluidx(c, U1, U0, B1, nx, ny, nz, 0, dt, nullptr, 1, Wy, 1));
-    // x, with the calcfl epilogue for the next step
-    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0, Wy));
     const size_t nparts = fluidx_parts(c);
     if (c->part.cap < nparts * c->ks->part_bytes)
         return MHD_ERR_ARG;
+    const int S = host_tail_slabs(c, Wy);
+    if (S > 1) {
+        // The last step of a host-buffer step: the y fluidx, the x advectbyzx
+        // and the x fluidx run on S slabs of planes along z, and each slab's
+        // b and u go out as soon as they are final.  The advectbyzx of planes
+        // k0..k1-1 reads its inputs at k0-1 .. k1 (C/advectbyzxB1.c: u at k-1;
+        // C/advectbyzxB2.c: b(1) at k takes the flux of plane k+1), and the
+        // x fluidx reads b at k1: the y fluidx runs one slab ahead (its last
+        // slab first, for the periodic neighbour of plane 0) and the x fluidx
+        // one slab behind the advectbyzx.
+        const int kc = nz / S;
+        auto yfluidx = [&](int s) {
+            SlabRange r(c, s * kc, kc);
+            return op_fluidx(c, U1, U0, B1, nx, ny, nz, 0, dt, nullptr, 1, Wy, 1);
+        };
+        auto xfluidx = [&](int s) {
+            {
+                SlabRange r(c, s * kc, kc);
+                MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, c->part.p, 0));
+            }
+            return copy_out(c, 0, s * kc, kc);
+        };
+        MHD_TRY(yfluidx(S - 1));
+        MHD_TRY(yfluidx(0));
+        for (int s = 0; s < S; s++) {
+            if (s + 1 < S - 1)
+                MHD_TRY(yfluidx(s + 1));
+            {
+                SlabRange r(c, s * kc, kc);
+                MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0, Wy));
+            }
+            MHD_TRY(copy_out(c, 1, s * kc, kc));
+            if (s > 0)
+                MHD_TRY(xfluidx(s - 1));
+        }
+        MHD_TRY(xfluidx(S - 1));
+        c->cfl_nparts = (int)nparts;
+        return MHD_OK;
+    }
+    MHD_TRY(op_fluidx(c, U1, U0, B1, nx, ny, nz, 0, dt, nullptr, 1, Wy, 1));
+    // x, with the calcfl epilogue for the next step
+    MHD_TRY(op_advect(c, B0, B1, U1, B1, nx, ny, nz, 0, dt, 0, Wy));
+    MHD_TRY(copy_out(c, 1));
     MHD_TRY(op_fluidx(c, U0, U1, B0, nx, ny, nz, 0, dt, c->part.p, 0));
+    MHD_TRY(copy_out(c, 0));
     c->cfl_nparts = (int)nparts;
     return MHD_OK;
 }
@@ -804,23 +920,110 @@ static int step_graph(mhd_ctx* c, double cfl, int variant)
     return MHD_OK;
 }
 
+// The grid and variant checks of a step.
+static int check_step(const mhd_ctx* c, int variant)
+{
+    if (variant == MHD_PLAIN && c->ny != c->nz)  // transpose13 is applied to (ny,nx,nz) and (nz,nx,ny)
+        return MHD_ERR_UNSUPPORTED;
+    if (variant == MHD_FUSED && !c->ks->fused_ok(c->nx, c->ny, c->nz))
+        return MHD_ERR_UNSUPPORTED;
+    MHD_TRY(check_dims(c->nx, c->ny, c->nz));
+    MHD_TRY(check_dims(c->ny, c->nx, c->nz));
+    MHD_TRY(check_dims(c->nz, c->nx, c->ny));
+    return MHD_OK;
+}
+
 extern "C" MHD_API int mhd_step(mhd_ctx* c, int nsteps, double cfl, int variant)
 {
     if (!c || !c->have_state || nsteps < 0 || !(cfl > 0) || (variant != MHD_PLAIN && variant != MHD_FUSED))
         return set_err(MHD_ERR_ARG);
-    if (variant == MHD_PLAIN && c->ny != c->nz)  // transpose13 is applied to (ny,nx,nz) and (nz,nx,ny)
-        return set_err(MHD_ERR_UNSUPPORTED);
-    if (variant == MHD_FUSED && !c->ks->fused_ok(c->nx, c->ny, c->nz))
-        return set_err(MHD_ERR_UNSUPPORTED);
-    MHD_TRY(set_err(check_dims(c->nx, c->ny, c->nz)));
-    MHD_TRY(set_err(check_dims(c->ny, c->nx, c->nz)));
-    MHD_TRY(set_err(check_dims(c->nz, c->nx, c->ny)));
+    MHD_TRY(set_err(check_step(c, variant)));
     for (int s = 0; s < nsteps; s++) {
         int st = (c->use_graphs && !c->profile) ? step_graph(c, cfl, variant) : step_once_direct(c, cfl, variant);
         if (st != MHD_OK)
             return set_err(st);
     }
     return set_err(MHD_OK);
+}
+
+static int ensure_copy_stream(mhd_ctx* c)
+{
+    if (!c->cstream)
+        CUDA_TRY(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
+    while ((int)c->cev.size() < kCevChunk0 + kHostChunks) {
+        cudaEvent_t e = nullptr;
+        CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->cev.push_back(e);
+    }
+    return MHD_OK;
+}
+
+// Steps on a host-resident state (the reference's loop, C/mhd.c:59-124, with
+// its arrays in host memory): u and b are copied in, stepped nsteps times and
+// the result is copied back into them; the call returns when it is there.
+// The copies overlap the step: the state comes in as kHostChunks chunks on a
+// copy stream and the compute stream runs the first CFL pass of each chunk
+// as it lands; the final b goes out while the last fluidx runs.  The
+// context's clock is kept (the state is assumed to be at its time t).
+extern "C" MHD_API int mhd_step_host(mhd_ctx* c, void* u, void* b, int nsteps, double cfl, int variant)
+{
+    if (!c || !u || !b || nsteps < 1 || !(cfl > 0) || (variant != MHD_PLAIN && variant != MHD_FUSED))
+        return set_err(MHD_ERR_ARG);
+    MHD_TRY(set_err(check_step(c, variant)));
+    MHD_TRY(set_err(ensure_state(c)));
+    MHD_TRY(set_err(ensure_copy_stream(c)));
+    if (!c->have_state)
+        MHD_TRY(mhd_set_time(c, 0.0, INFINITY));
+    const size_t cells = ncell(c), eu = 5 * (size_t)c->elem, eb = 3 * (size_t)c->elem;
+    char* U0 = static_cast<char*>(c->U[0].p);
+    char* B0 = static_cast<char*>(c->B[0].p);
+    const char* hu = static_cast<const char*>(u);
+    const char* hb = static_cast<const char*>(b);
+    // the copies start after the work already queued on the compute stream
+    if (cudaEventRecord(c->cev[kCevEntry], c->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(c->cstream, c->cev[kCevEntry], 0) != cudaSuccess)
+        return set_err(MHD_ERR_CUDA);
+    // chunks of whole CFL partials (256 cells), so chunk k's partials follow chunk k-1's
+    size_t chunk = (cells + kHostChunks - 1) / kHostChunks;
+    chunk = (chunk + 255) / 256 * 256;
+    for (int k = 0; k < kHostChunks; k++) {
+        const size_t c0 = (size_t)k * chunk;
+        if (c0 >= cells)
+            break;
+        const size_t n = (cells - c0 < chunk) ? cells - c0 : chunk;
+        if (cudaMemcpyAsync(U0 + c0 * eu, hu + c0 * eu, n * eu, cudaMemcpyDefault, c->cstream) != cudaSuccess ||
+            cudaMemcpyAsync(B0 + c0 * eb, hb + c0 * eb, n * eb, cudaMemcpyDefault, c->cstream) != cudaSuccess ||
+            cudaEventRecord(c->cev[kCevChunk0 + k], c->cstream) != cudaSuccess ||
+            cudaStreamWaitEvent(c->stream, c->cev[kCevChunk0 + k], 0) != cudaSuccess)
+            return set_err(MHD_ERR_CUDA);
+        int np = 0;
+        KTimer kt(c, MHD_K_CALCFL);
+        if (c->ks->calcfl(U0 + c0 * eu, B0 + c0 * eb, n, c0,
+                          static_cast<char*>(c->part.p) + (c0 / 256) * c->ks->part_bytes, &np, BoxStrides{},
+                          c->stream) != cudaSuccess)
+            return set_err(MHD_ERR_CUDA);
+    }
+    c->cfl_nparts = (int)((cells + 255) / 256);
+    c->cfl_valid = true;
+    c->have_state = true;
+    int st = MHD_OK;
+    for (int s = 0; s < nsteps && st == MHD_OK; s++) {
+        if (s + 1 == nsteps) {  // the last step copies its result out as it is produced
+            c->out_u = u;
+            c->out_b = b;
+            st = step_once_direct(c, cfl, variant);
+            c->out_u = c->out_b = nullptr;
+        } else {
+            st = (c->use_graphs && !c->profile) ? step_graph(c, cfl, variant) : step_once_direct(c, cfl, variant);
+        }
+    }
+    // later work on the compute stream waits for the copies out
+    const bool ok = cudaEventRecord(c->cev[kCevDone], c->cstream) == cudaSuccess &&
+                    cudaStreamWaitEvent(c->stream, c->cev[kCevDone], 0) == cudaSuccess;
+    const bool synced = cudaStreamSynchronize(c->cstream) == cudaSuccess;
+    if (st != MHD_OK)
+        return set_err(st);
+    return set_err((ok && synced) ? MHD_OK : MHD_ERR_CUDA);
 }
 
 extern "C" MHD_API int mhd_use_graphs(mhd_ctx* c, int enable)

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
     __shared__ uint64_t full[2];
 
     const int ny = a.ny, nz = a.nz, K = a.K;
-    const int j0 = blockIdx.x * J, k0 = blockIdx.y * K;
+    const int j0 = blockIdx.x * J, k0 = a.kbeg + blockIdx.y * K;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const bool halo = (w == J);
     const Group<float, T> g(tid);

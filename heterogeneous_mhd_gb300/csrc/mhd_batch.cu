@@ -266,7 +266,7 @@ static int cfl_first_pass(mhd_batch* b)
 {
     for (auto& c : b->cls) {
         int np = 0;
-        BTRY(cu(b->ks->calcfl(c.U[0], c.B[0], c.cells(), c.part, &np, strides(b, c), b->stream)));
+        BTRY(cu(b->ks->calcfl(c.U[0], c.B[0], c.cells(), 0, c.part, &np, strides(b, c), b->stream)));
         c.cfl_nparts = np;
         b->launches++;
     }

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
     const int lp = tid / T;  // local pencil
     const Group<R, T> g(tid);
     const int i0 = g.t * C;
-    const int j0 = blockIdx.x * P, k = blockIdx.y;
+    const int j0 = blockIdx.x * P, k = a.kbeg + blockIdx.y;  // k: plane along z (x sweep)
     const int kp = (k + 1 == a.nz) ? 0 : k + 1;
     const int jn = (j0 + P == a.ny) ? 0 : j0 + P;
 
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
     } else {
         // the rows of the group (x0..x0+P-1) along the whole pencil at plane kk,
         // its b rows at plane kn, and the b of cell x0+P (periodic)
-        const int x0 = blockIdx.x * P, kk = blockIdx.y;
+        const int x0 = blockIdx.x * P, kk = a.kbeg + blockIdx.y;
         const int nk = (AX == 1) ? a.nz : a.ny;
         const int kn = (kk + 1 == nk) ? 0 : kk + 1;
         const int xn = (x0 + P == a.nx) ? 0 : x0 + P;
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
                 cm = fmax(cm, red[s]);
                 lnan = max(lnan, rn[s]);
             }
-            CflPart<R>* part = static_cast<CflPart<R>*>(a.cfl_part) + (blockIdx.y * gridDim.x + blockIdx.x);
+            CflPart<R>* part = static_cast<CflPart<R>*>(a.cfl_part) + ((size_t)k * gridDim.x + blockIdx.x);
             part->cmax = cm;
             part->last_nan = lnan;
         }
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
-            const int x0 = blockIdx.x * P, kk = blockIdx.y;
+            const int x0 = blockIdx.x * P, kk = a.kbeg + blockIdx.y;
 #pragma unroll
             for (int h = 0; h < NBX; h++) {
                 const int py = (AX == 1) ? h * BXR : kk, pz = (AX == 1) ? kk : h * BXR;

@@ -49,6 +49,8 @@ struct FluidxArgs {
     void* w_out;          // optional (FP32): (rho, m) of the new state, 2 values per cell, x-major:
                           // m = m_x on the x sweep, on the y/z sweeps the momentum component w_comp
     int w_comp;           // y/z sweeps: raw component of u written with rho (1 m_x, 2 m_y, 3 m_z)
+    int kbeg, kcount;     // planes along z to update: kbeg .. kbeg+kcount-1 (kcount 0: all); the
+                          // neighbours of the range's edge planes are read as usual (periodic box)
 };
 
 struct AdvectArgs {
@@ -66,6 +68,7 @@ struct AdvectArgs {
     int axis;             // sweep axis of the untransposed state: 0 x (the drop-in call), 1 y, 2 z
     const void* w;        // optional (FP32): (rho, m_d) of update_u, 2 values per cell, x-major, m_d the
                           // momentum along the sweep (the fluidx before wrote it)
+    int kbeg, kcount;     // planes along z to update (kcount 0: all), as in FluidxArgs
 };
 
 struct TransposeArgs {
@@ -669,10 +672,10 @@ static __global__ void __launch_bounds__(256) k_copy4(const float* __restrict__ 
 
 // calcfl (C/calcfl.c:13-63), first pass: per-CTA max of the per-cell speed
 // over a contiguous range of cells (blockDim cells per CTA) and the last NaN
-// index in the range.
+// index in the range (cell0 + the index in the range: the index in the box).
 template <typename R, bool EX>
 __global__ void __launch_bounds__(256) k_calcfl(const R* __restrict__ u, const R* __restrict__ b, size_t ncell,
-                                                CflPart<R>* part, BoxStrides bs)
+                                                size_t cell0, CflPart<R>* part, BoxStrides bs)
 {
     __shared__ R rm[8];
     __shared__ int rn[8];
@@ -695,7 +698,7 @@ __global__ void __launch_bounds__(256) k_calcfl(const R* __restrict__ u, const R
         isn = (sp != sp);
     }
     R m = warp_max<R>(isn ? R(0) : sp);
-    int ln = isn ? (int)cell : -1;
+    int ln = isn ? (int)(cell0 + cell) : -1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
         ln = max(ln, __shfl_xor_sync(0xffffffffu, ln, o));

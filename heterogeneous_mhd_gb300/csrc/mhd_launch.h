@@ -15,9 +15,11 @@ struct KernelSet {
     cudaError_t (*fluidx)(const FluidxArgs&, cudaStream_t);
     cudaError_t (*advect)(const AdvectArgs&, cudaStream_t);
     cudaError_t (*transpose)(const TransposeArgs&, cudaStream_t);
-    // first CFL pass over ncell cells; returns the number of partials written
-    cudaError_t (*calcfl)(const void* u, const void* b, size_t ncell, void* part, int* nparts, const BoxStrides& bs,
-                          cudaStream_t);
+    // first CFL pass over ncell cells, the first of which is cell cell0 of the
+    // box (NaN cells are reported by their index in the box); returns the
+    // number of partials written
+    cudaError_t (*calcfl)(const void* u, const void* b, size_t ncell, size_t cell0, void* part, int* nparts,
+                          const BoxStrides& bs, cudaStream_t);
     cudaError_t (*cfl_finalize)(const CflFinalizeArgs&, cudaStream_t);
     cudaError_t (*divb)(const void* b, int nx, int ny, int nz, double* part, int* nparts, cudaStream_t);
     size_t part_bytes; // sizeof(CflPart<R>)
@@ -31,6 +33,10 @@ struct KernelSet {
     int (*transpose_writes_w)(int axis, int nx, int ny, int nz);
     // nonzero if the fused step's fluidx sweep along `axis` (1: y) writes it
     int (*sweep_writes_w)(int axis, int nx, int ny, int nz);
+    // nonzero if the fused step's last three operators (the y-sweep fluidx,
+    // the x-sweep advectbyzx with the side array and the x-sweep fluidx) take
+    // ranges of kcount planes along z (FluidxArgs/AdvectArgs::kbeg, kcount)
+    int (*tail_slabs_ok)(int nx, int ny, int nz, int kcount);
 };
 
 const KernelSet* kernels_f32_fast();

@@ -134,6 +134,16 @@ MHD_API int mhd_clock_ptr(mhd_ctx *ctx, void **clock);
  * (C/mhd.c:59-124) with dt = cfl * calcfl, clamped so that t never passes tf
  * (set by mhd_set_time; +inf by default).  Asynchronous. */
 MHD_API int mhd_step(mhd_ctx *ctx, int nsteps, double cfl, int variant);
+/* nsteps steps (as mhd_step) on a state held in host memory, which is what
+ * the reference's loop does (C/mhd.c:59-124 on the host arrays u, b): u
+ * (5*nx*ny*nz) and b (3*nx*ny*nz) are copied in, stepped, and the result is
+ * written back into them before the call returns.  The copies overlap the
+ * step (the first CFL pass runs on each chunk of the state as it arrives, b
+ * goes back out while the last fluidx runs); pinned host memory gives the
+ * full host-link bandwidth.  Equivalent to mhd_set_state, mhd_step and
+ * mhd_get_state, bit for bit, except that the context's clock (t, step
+ * count) carries on instead of restarting at t = 0. */
+MHD_API int mhd_step_host(mhd_ctx *ctx, void *u, void *b, int nsteps, double cfl, int variant);
 MHD_API int mhd_set_time(mhd_ctx *ctx, double t, double tf);
 MHD_API int mhd_get_time(mhd_ctx *ctx, double *t, double *dt, long long *steps);
 /* Capture each step variant into a CUDA graph on first use (default on). */
