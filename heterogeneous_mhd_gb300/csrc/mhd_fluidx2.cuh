@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
     R* const sf = AX ? su + fluidx_sweep_regb(n) : nullptr;      // y/z: [P][SF]
     R* const red = AX ? sf + P * SB : sbk + P * SB;
     R* const seam = red + 32;
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar, bar_u;  // bar_u: the u rows of a sweep along y or z
 
     const R* uu = static_cast<const R*>(a.uu);
     const R* ub = static_cast<const R*>(a.ub);
@@ -138,57 +138,91 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
         R* const rows_b = su;                          // [n][3P]
         R* const rows_bk = rows_b + n * 3 * kSweepP;   // [n][3P]
         R* const rows_bn = rows_bk + n * 3 * kSweepP;  // [n][4]
+        // two barriers: the b rows (bar) land before the u rows (bar_u), so the
+        // field pass runs while u is still arriving
         if (tid == 0) {
             mbar_init(&bar, 1);
-            mbar_arrive_expect_tx(&bar, (uint32_t)(n * (5 * kSweepP + 6 * kSweepP + 4) * sizeof(R)));
+            mbar_init(&bar_u, 1);
+            mbar_arrive_expect_tx(&bar, (uint32_t)(n * (6 * kSweepP + 4) * sizeof(R)));
+            mbar_arrive_expect_tx(&bar_u, (uint32_t)(n * 5 * kSweepP * sizeof(R)));
             // coordinates (x word, y, z): the pencil runs along y (AX 1) or z (AX 2) from 0
             const int y = (AX == 1) ? 0 : kk, z = (AX == 1) ? kk : 0;
             const int yk = (AX == 1) ? 0 : kn, zk = (AX == 1) ? kn : 0;
 #pragma unroll
             for (int h = 0; h < NBX; h++) {  // rows h*BXR.. of the pencil
                 const int dy = (AX == 1) ? h * BXR : 0, dz = (AX == 1) ? 0 : h * BXR;
-                tma_load_3d(rows_u + h * BXR * 5 * kSweepP, &tm.u_in, 5 * x0, y + dy, z + dz, &bar);
                 tma_load_3d(rows_b + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, y + dy, z + dz, &bar);
-                tma_load_3d(rows_bk + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, yk + dy, zk + dz, &bar);
                 tma_load_3d(rows_bn + h * BXR * 4, &tm.bn_in, 3 * xn, y + dy, z + dz, &bar);
+                tma_load_3d(rows_bk + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, yk + dy, zk + dz, &bar);
+            }
+#pragma unroll
+            for (int h = 0; h < NBX; h++) {
+                const int dy = (AX == 1) ? h * BXR : 0, dz = (AX == 1) ? 0 : h * BXR;
+                tma_load_3d(rows_u + h * BXR * 5 * kSweepP, &tm.u_in, 5 * x0, y + dy, z + dz, &bar_u);
             }
         }
         __syncthreads();
         if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
             return;  // a copy never landed (error bit set)
+        // Each thread takes the cells e = tid + it * NT (it < IT): cell (e / P, e % P).
+        // Every pass issues all of its loads before its stores.
+        constexpr int NT = kSweepP * T, IT = n * kSweepP / NT;
         // cell-centred field (C/fluidx.c:71-81) of cell (r, p), seen in the
         // transposed order: b_d averaged with the next row, b_x with the next
-        // pencil, b_k with the next plane.  Thread e takes cell (e / P, e % P):
-        // the staged rows are read at a stride of three words, sf is written
-        // with a pencil stride of 8 (mod 32) words, both without bank conflicts.
+        // pencil, b_k with the next plane.  The staged rows are read at a
+        // stride of three words, sf is written with a pencil stride of 8
+        // (mod 32) words, both without bank conflicts.
         constexpr int B0 = sweep_b<AX>(0), B1 = sweep_b<AX>(1), B2 = sweep_b<AX>(2);
-        for (int e = tid; e < n * kSweepP; e += blockDim.x) {
-            const int r = e / kSweepP, p = e - r * kSweepP;
-            const int rn = (r + 1 == n) ? 0 : r + 1;
-            const R* bc = rows_b + r * 3 * kSweepP + 3 * p;
-            const R bd = bc[B0], bdn = rows_b[rn * 3 * kSweepP + 3 * p + B0];
-            const R bj = bc[B1], bjn = (p + 1 < kSweepP) ? bc[3 + B1] : rows_bn[r * 4 + B1];
-            const R bk = bc[B2], bkn = rows_bk[r * 3 * kSweepP + 3 * p + B2];
-            R* o = sf + p * SB + 3 * r;
-            if constexpr (EX) {
-                o[0] = R(0.5) * bd + R(0.5) * bdn;
-                o[1] = R(0.5) * bj + bjn / R(2);
-                o[2] = R(0.5) * bk + bkn / R(2);
-            } else {  // the same values: halving is exact
-                o[0] = R(0.5) * (bd + bdn);
-                o[1] = R(0.5) * (bj + bjn);
-                o[2] = R(0.5) * (bk + bkn);
+        {
+            R fv[IT][6];
+#pragma unroll
+            for (int it = 0; it < IT; it++) {
+                const int e = tid + it * NT, r = e / kSweepP, p = e - r * kSweepP;
+                const int rn = (r + 1 == n) ? 0 : r + 1;
+                const R* bc = rows_b + r * 3 * kSweepP + 3 * p;
+                fv[it][0] = bc[B0];
+                fv[it][1] = rows_b[rn * 3 * kSweepP + 3 * p + B0];
+                fv[it][2] = bc[B1];
+                fv[it][3] = (p + 1 < kSweepP) ? bc[3 + B1] : rows_bn[r * 4 + B1];
+                fv[it][4] = bc[B2];
+                fv[it][5] = rows_bk[r * 3 * kSweepP + 3 * p + B2];
+            }
+#pragma unroll
+            for (int it = 0; it < IT; it++) {
+                const int e = tid + it * NT, r = e / kSweepP, p = e - r * kSweepP;
+                R* o = sf + p * SB + 3 * r;
+                if constexpr (EX) {
+                    o[0] = R(0.5) * fv[it][0] + R(0.5) * fv[it][1];
+                    o[1] = R(0.5) * fv[it][2] + fv[it][3] / R(2);
+                    o[2] = R(0.5) * fv[it][4] + fv[it][5] / R(2);
+                } else {  // the same values: halving is exact
+                    o[0] = R(0.5) * (fv[it][0] + fv[it][1]);
+                    o[1] = R(0.5) * (fv[it][2] + fv[it][3]);
+                    o[2] = R(0.5) * (fv[it][4] + fv[it][5]);
+                }
             }
         }
-        __syncthreads();  // the staged b is dead: su takes its place
+        // the staged b is dead (su takes its place) once every thread is here and u has landed
+        if (!__syncthreads_and(mbar_wait_bounded(&bar_u, 0, a.err)))
+            return;
         // u rows -> pencil-major, raw component order (stride-5 reads, 8 (mod 32) pencil stride)
-        for (int e = tid; e < n * kSweepP; e += blockDim.x) {
-            const int r = e / kSweepP, p = e - r * kSweepP;
-            const R* src = rows_u + 5 * e;
-            R* dst = su + p * SU + 5 * r;
+        {
+            R uv[IT][5];
 #pragma unroll
-            for (int c = 0; c < 5; c++)
-                dst[c] = src[c];
+            for (int it = 0; it < IT; it++) {
+                const R* src = rows_u + 5 * (tid + it * NT);
+#pragma unroll
+                for (int c = 0; c < 5; c++)
+                    uv[it][c] = src[c];
+            }
+#pragma unroll
+            for (int it = 0; it < IT; it++) {
+                const int e = tid + it * NT, r = e / kSweepP, p = e - r * kSweepP;
+                R* dst = su + p * SU + 5 * r;
+#pragma unroll
+                for (int c = 0; c < 5; c++)
+                    dst[c] = uv[it][c];
+            }
         }
         __syncthreads();
     }
@@ -475,16 +509,26 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
         __syncthreads();
         R* const rows_w = sf;  // [n][2P]
         const int wc = a.w_out ? a.w_comp : 0;
-        for (int e = tid; e < n * kSweepP; e += blockDim.x) {
-            const int r = e / kSweepP, p = e - r * kSweepP;
+        constexpr int NT = kSweepP * T, IT = n * kSweepP / NT;
+        R uv[IT][5];
+#pragma unroll
+        for (int it = 0; it < IT; it++) {
+            const int e = tid + it * NT, r = e / kSweepP, p = e - r * kSweepP;
             const R* src = su + p * SU + 5 * r;
+#pragma unroll
+            for (int c = 0; c < 5; c++)
+                uv[it][c] = src[c];
+        }
+#pragma unroll
+        for (int it = 0; it < IT; it++) {
+            const int e = tid + it * NT;
             R* dst = rows_u + 5 * e;
 #pragma unroll
             for (int c = 0; c < 5; c++)
-                dst[c] = src[c];
+                dst[c] = uv[it][c];
             if (wc) {
-                rows_w[2 * e] = src[0];
-                rows_w[2 * e + 1] = src[wc];
+                rows_w[2 * e] = uv[it][0];
+                rows_w[2 * e + 1] = (wc == 1) ? uv[it][1] : ((wc == 2) ? uv[it][2] : uv[it][3]);
             }
         }
         fence_proxy_async_smem();
