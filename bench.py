@@ -66,6 +66,7 @@ MOVED_BYTES = {"plain": {"fluidx": 52 + 8 * 3 / 6, "advectbyzx": 32, "transpose1
 STEP_BYTES = {"plain": 864, "fused": 576, "fused_5pass": 320}
 STEP_MOVED = {"plain": 6 * 52 + 3 * 8 + 6 * 32 + 4 * 64 + 2 * 8, "fused": 6 * 52 + 5 * 8 + 6 * 32}
 METRIC = "cell-updates/s at 256^3 (plain vs fused); closure speedup at matched error"
+E2E_TRIALS = 5
 
 
 def dist_env():
@@ -549,27 +550,35 @@ def our_arm(args):
     hb.numpy()[:] = b0
     e2e_steps = max(3, min(args.steps, 10))
     ctx.step_host(hu, hb, 1, cfl=0.7, fused=(main == "fused"))  # warm-up (the copy stream's first use)
-    hu.numpy()[:] = u0
-    hb.numpy()[:] = b0
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        # H2D from pinned memory, one step, D2H into the same buffers (synchronous)
-        ctx.step_host(hu, hb, 1, cfl=0.7, fused=(main == "fused"))
-    e2e_s = time.perf_counter() - t0
-    # the same with the three calls and no overlap of the copies with the step
-    hu.numpy()[:] = u0
-    hb.numpy()[:] = b0
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ctx.set_state(hu, hb)
-        ctx.step(1, cfl=0.7, fused=(main == "fused"))
-        ctx.get_state_into(hu, hb)
-    e2e3_s = time.perf_counter() - t0
-    (e2e_s, e2e3_s) = rep.max([e2e_s, e2e3_s])
-    e2e = world * cells * e2e_steps / e2e_s
-    e2e3 = world * cells * e2e_steps / e2e3_s
+    # The host link is shared with the rest of the machine and its speed varies
+    # from second to second: E2E_TRIALS interleaved trials of both paths, the
+    # median trial of each is reported (all trials are listed).
+    t_host, t_three = [], []
+    for _ in range(E2E_TRIALS):
+        hu.numpy()[:] = u0
+        hb.numpy()[:] = b0
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            # H2D from pinned memory, one step, D2H into the same buffers (synchronous)
+            ctx.step_host(hu, hb, 1, cfl=0.7, fused=(main == "fused"))
+        t_host.append(time.perf_counter() - t0)
+        # the same with the three calls and no overlap of the copies with the step
+        hu.numpy()[:] = u0
+        hb.numpy()[:] = b0
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ctx.set_state(hu, hb)
+            ctx.step(1, cfl=0.7, fused=(main == "fused"))
+            ctx.get_state_into(hu, hb)
+        t_three.append(time.perf_counter() - t0)
+    t_host = rep.max(t_host)
+    t_three = rep.max(t_three)
+    e2e = world * cells * e2e_steps / statistics.median(t_host)
+    e2e3 = world * cells * e2e_steps / statistics.median(t_three)
+    e2e_trials = {"mhd_step_host": [world * cells * e2e_steps / t for t in t_host],
+                  "three_calls": [world * cells * e2e_steps / t for t in t_three]}
     if rank != 0:
         ctx.close()
         rep.close()
@@ -594,7 +603,8 @@ def our_arm(args):
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": 32 * cells,
                 "d2h_bytes_per_step": 32 * cells, "steps": e2e_steps,
                 "api": "mhd_step_host (copies overlapped with the step)",
-                "three_calls_value": e2e3, "three_calls_api": "mhd_set_state + mhd_step + mhd_get_state"},
+                "three_calls_value": e2e3, "three_calls_api": "mhd_set_state + mhd_step + mhd_get_state",
+                "trials": e2e_trials, "statistic": f"median of {E2E_TRIALS} interleaved trials of {e2e_steps} steps"},
         "roofline": roof,
         "kernels": head["kernels"],
         "profiled_ms_per_step": ms_profiled / args.steps,

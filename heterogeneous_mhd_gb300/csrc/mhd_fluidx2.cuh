@@ -112,6 +112,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
     const size_t c0 = ((size_t)k * a.ny + j0) * n;
     const size_t cn = ((size_t)k * a.ny + jn) * n;
     const size_t ck = ((size_t)kp * a.ny + j0) * n;
+    const R dt = load_dt<R>(a.dt_ptr, a.dt_val);  // read while the tensor copies land
 
     if constexpr (AX == 0) {
         if (tid == 0) {
@@ -227,7 +228,6 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
         __syncthreads();
     }
 
-    const R dt = load_dt<R>(a.dt_ptr, a.dt_val);
     using W = wide_t<R, EX>;
 
     // ---- gather this thread's cells.  q and the cell-centred field are read
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
         if (tid == 0) {
             tma_store_1d(static_cast<R*>(a.u_out) + c0 * 5, su, 5u * np * sizeof(R));
             tma_store_commit();
-            tma_store_wait_all();
+            tma_store_wait_read();  // the CTA may leave once its buffers are read
         }
     } else {
         // pencil-major -> rows (the mapping of the gather, reversed), then one
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
                     tma_store_3d(&tm.w_out, 2 * x0, py, pz, rows_w + h * BXR * 2 * kSweepP);
             }
             tma_store_commit();
-            tma_store_wait_all();
+            tma_store_wait_read();  // the CTA may leave once its buffers are read
         }
     }
 }
