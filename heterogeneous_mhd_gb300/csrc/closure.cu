@@ -832,49 +832,119 @@ __global__ void __launch_bounds__(WgradShape<CIN, COUTP, KS>::THREADS)
     }
 }
 
-// out[e] = sum_p part[p * stride + e], e < len (fixed order: deterministic)
-__global__ void k_sum_parts(const float* __restrict__ part, int nparts, size_t stride, size_t len,
-                            float* __restrict__ out)
+// Partial sums of reductions: a CTA of kSumWarps warps takes 32 consecutive
+// output elements; warp w sums the partials p = w, w + kSumWarps, ... of its
+// lane's element and the warps' sums are added in warp order (a fixed order:
+// deterministic).
+constexpr int kSumWarps = 8;
+
+// out[e] = sum_p part[p * stride + e], e < len; launched on (len + 31) / 32 CTAs of kSumWarps warps
+__global__ void __launch_bounds__(kSumWarps * 32) k_sum_parts(const float* __restrict__ part, int nparts,
+                                                             size_t stride, size_t len, float* __restrict__ out)
 {
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < len; e += (size_t)gridDim.x * blockDim.x) {
-        float s = 0.f;
-        for (int p = 0; p < nparts; p++)
+    __shared__ float red[kSumWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t e = (size_t)blockIdx.x * 32 + lane;
+    float s = 0.f;
+    if (e < len)
+        for (int p = w; p < nparts; p += kSumWarps)
             s += part[(size_t)p * stride + e];
-        out[e] = s;
+    red[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && e < len) {
+        float t = 0.f;
+#pragma unroll
+        for (int k = 0; k < kSumWarps; k++)
+            t += red[k][lane];
+        out[e] = t;
     }
 }
 
 // weight-gradient partials part[p][tap][cop][cip] summed into the master
-// layout dw[co][tap][ci] for co < cor, ci < cir
-__global__ void k_wsum(const float* __restrict__ part, int nparts, int taps, int cop, int cip, int cor, int cir,
-                       float* __restrict__ dw)
+// layout dw[co][tap][ci] for co < cor, ci < cir, in the order of k_sum_parts
+// (a coalesced 128-byte row per partial and warp)
+constexpr int kWsumWarps = kSumWarps;
+__global__ void __launch_bounds__(kWsumWarps * 32) k_wsum(const float* __restrict__ part, int nparts, int taps,
+                                                         int cop, int cip, int cor, int cir, float* __restrict__ dw)
 {
+    __shared__ float red[kWsumWarps][32];
     const size_t len = (size_t)cor * taps * cir, stride = (size_t)taps * cop * cip;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < len; e += (size_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t e = (size_t)blockIdx.x * 32 + lane;
+    float s = 0.f;
+    if (e < len) {
         const int ci = (int)(e % cir), tap = (int)((e / cir) % taps), co = (int)(e / ((size_t)cir * taps));
-        const size_t src = ((size_t)tap * cop + co) * cip + ci;
-        float s = 0.f;
-        for (int p = 0; p < nparts; p++)
-            s += part[(size_t)p * stride + src];
-        dw[e] = s;
+        const float* src = part + ((size_t)tap * cop + co) * cip + ci;
+        float s0 = 0.f, s1 = 0.f;  // two chains: more loads in flight
+        int p = w;
+        for (; p + kWsumWarps < nparts; p += 2 * kWsumWarps) {
+            s0 += src[(size_t)p * stride];
+            s1 += src[(size_t)(p + kWsumWarps) * stride];
+        }
+        if (p < nparts)
+            s0 += src[(size_t)p * stride];
+        s = s0 + s1;
+    }
+    red[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && e < len) {
+        float t = 0.f;
+#pragma unroll
+        for (int k = 0; k < kWsumWarps; k++)
+            t += red[k][lane];
+        dw[e] = t;
     }
 }
 
-// column sums of a [count][C] bf16 tensor: per-block partials part[block][C]
-__global__ void k_colsum(const bf16* __restrict__ x, int C, size_t count, float* __restrict__ part)
+// column sums of a [count][C] bf16 tensor (C = 8, 16 or 32): per-block
+// partials part[block][C].  Thread t reads 16-byte chunks (8 channels) of
+// chunk column t % (C/8), four rows per iteration in flight; lanes of the
+// same chunk column are summed by shuffles, then the warps in warp order.
+__global__ void __launch_bounds__(256) k_colsum(const bf16* __restrict__ x, int C, size_t count,
+                                                float* __restrict__ part)
 {
-    extern __shared__ float red[];
-    const int c = threadIdx.x % C, lane_rows = blockDim.x / C, r0 = threadIdx.x / C;
-    float s = 0.f;
-    if (r0 < lane_rows)
-        for (size_t v = blockIdx.x * (size_t)lane_rows + r0; v < count; v += (size_t)gridDim.x * lane_rows)
-            s += __bfloat162float(x[v * C + c]);
-    red[threadIdx.x] = s;
+    __shared__ float red[8][32];
+    const int Q = C / 8;  // 16-byte chunks per row
+    const int q = threadIdx.x % Q, rows = blockDim.x / Q, r0 = threadIdx.x / Q;
+    const size_t stride = (size_t)gridDim.x * rows;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    auto add = [&](const uint4& v) {
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float2 f = __bfloat1622float2(h[k]);
+            acc[2 * k] += f.x;
+            acc[2 * k + 1] += f.y;
+        }
+    };
+    const uint4* x4 = reinterpret_cast<const uint4*>(x);
+    size_t v = blockIdx.x * (size_t)rows + r0;
+    for (; v + 3 * stride < count; v += 4 * stride) {
+        const uint4 a0 = __ldg(x4 + v * Q + q), a1 = __ldg(x4 + (v + stride) * Q + q);
+        const uint4 a2 = __ldg(x4 + (v + 2 * stride) * Q + q), a3 = __ldg(x4 + (v + 3 * stride) * Q + q);
+        add(a0);
+        add(a1);
+        add(a2);
+        add(a3);
+    }
+    for (; v < count; v += stride)
+        add(__ldg(x4 + v * Q + q));
+    // lanes l and l ^ o (o >= Q) hold the same chunk column
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        for (int o = 16; o >= Q; o >>= 1)
+            acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane < Q) {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            red[w][lane * 8 + k] = acc[k];
+    }
     __syncthreads();
     if (threadIdx.x < C) {
         float t = 0.f;
-        for (int r = 0; r < lane_rows; r++)
-            t += red[r * C + threadIdx.x];
+        for (int s = 0; s < (int)(blockDim.x >> 5); s++)
+            t += red[s][threadIdx.x];
         part[(size_t)blockIdx.x * C + threadIdx.x] = t;
     }
 }
@@ -896,9 +966,13 @@ __global__ void k_loss1(const float* __restrict__ out, const bf16* __restrict__ 
     for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(v % n), j = (int)((v / n) % n), k = (int)((v / ((size_t)n * n)) % n);
         const int box = (int)(v / ((size_t)n * n * n));
-        const float* o = out + v * 8;
-        const bf16* tg = tgt + v * 8;
-        bf16* d = dout + v * 16;
+        // the voxel's row: 8 FP32 outputs, 8 BF16 targets, 16 BF16 gradients (16-byte accesses)
+        const float4 o0 = *reinterpret_cast<const float4*>(out + v * 8);
+        const float4 o1 = *reinterpret_cast<const float4*>(out + v * 8 + 4);
+        const uint4 t4 = *reinterpret_cast<const uint4*>(tgt + v * 8);
+        const bf16* tg = reinterpret_cast<const bf16*>(&t4);
+        const float o[8] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
+        __align__(16) bf16 d[16];
 #pragma unroll
         for (int c = 0; c < 5; c++) {
             const float r = o[c] - __bfloat162float(tg[c]);
@@ -908,6 +982,9 @@ __global__ void k_loss1(const float* __restrict__ out, const bf16* __restrict__ 
 #pragma unroll
         for (int c = 5; c < 16; c++)
             d[c] = __float2bfloat16_rn(0.f);
+        uint4* d4 = reinterpret_cast<uint4*>(dout + v * 16);
+        d4[0] = reinterpret_cast<const uint4*>(d)[0];
+        d4[1] = reinterpret_cast<const uint4*>(d)[1];
         const float* oi = out + vidx(box, k, j, i + 1 == n ? 0 : i + 1, n) * 8;
         const float* oj = out + vidx(box, k, j + 1 == n ? 0 : j + 1, i, n) * 8;
         const float* ok = out + vidx(box, k + 1 == n ? 0 : k + 1, j, i, n) * 8;
@@ -1368,8 +1445,8 @@ int launch_wgrad(const void* a, const void* dz, float* part, float* dw, int cor,
     if (cudaGetLastError() != cudaSuccess)
         return MHD_ERR_CUDA;
     const size_t len = (size_t)cor * S::TAPS * cir;
-    k_wsum<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(part, (int)(grid * S::WK), S::TAPS, COUTP, CIN, cor, cir,
-                                                          dw);
+    k_wsum<<<(unsigned)((len + 31) / 32), kWsumWarps * 32, 0, s>>>(part, (int)(grid * S::WK), S::TAPS, COUTP, CIN,
+                                                                    cor, cir, dw);
     return st(cudaGetLastError());
 }
 
@@ -1471,12 +1548,14 @@ extern "C" MHD_API int mhd_cl_colsum(const void* x, int channels, long long coun
         nout > channels)
         return MHD_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int threads = 256, blocks = 256;
-    k_colsum<<<blocks, threads, threads * sizeof(float), s>>>(static_cast<const bf16*>(x), channels, (size_t)count,
-                                                              scratch);
+    const int threads = 256, blocks = 256;  // blocks: the scratch holds 256 * channels partials
+    if (reinterpret_cast<uintptr_t>(x) & 15)
+        return MHD_ERR_ARG;  // rows are read as 16-byte chunks
+    k_colsum<<<blocks, threads, 0, s>>>(static_cast<const bf16*>(x), channels, (size_t)count, scratch);
     if (cudaGetLastError() != cudaSuccess)
         return MHD_ERR_CUDA;
-    k_sum_parts<<<1, 32, 0, s>>>(scratch, blocks, (size_t)channels, (size_t)nout, out);
+    k_sum_parts<<<(unsigned)((nout + 31) / 32), kSumWarps * 32, 0, s>>>(scratch, blocks, (size_t)channels,
+                                                                        (size_t)nout, out);
     return st(cudaGetLastError());
 }
 
@@ -1485,6 +1564,9 @@ extern "C" MHD_API int mhd_cl_loss(const float* out, const void* target, void* d
 {
     if (!out || !target || !dout || !rb_scratch || !loss_scratch || !loss || !shape_ok(nb, n))
         return MHD_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(target) | reinterpret_cast<uintptr_t>(dout)) &
+        15)
+        return MHD_ERR_ARG;  // rows are moved in 16-byte pieces
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t nv = (size_t)nb * n * n * n;
     const float gscale = 2.0f / (8.0f * (float)nv);
@@ -1496,7 +1578,7 @@ extern "C" MHD_API int mhd_cl_loss(const float* out, const void* target, void* d
     k_loss2<<<blocks_for(nv, 256), 256, 0, s>>>(rb_scratch, static_cast<bf16*>(dout), nb, n, gscale);
     if (cudaGetLastError() != cudaSuccess)
         return MHD_ERR_CUDA;
-    k_sum_parts<<<1, 32, 0, s>>>(loss_scratch, (int)blocks, 1, 1, loss);  // sum of squares; /(8N) on the host
+    k_sum_parts<<<1, kSumWarps * 32, 0, s>>>(loss_scratch, (int)blocks, 1, 1, loss);  // sum of squares; /(8N) on the host
     return st(cudaGetLastError());
 }
 
