@@ -437,7 +437,9 @@ static bool plan_advect6(const AdvectArgs& a, bool aligned, A6Plan& p)
     const int kn = tune_value(TUNE_ADVECT_KERNEL);
     if (!kV2 || !aligned || a.axis != 0 || !(kn == 6 || (kn == 0 && (a.nx == 128 || a.nx == 256))))
         return false;
-    if (a.w == nullptr || (reinterpret_cast<uintptr_t>(a.w) & 15) != 0 || a.b1_src != a.ub || a.bs.count != 1)
+    // several boxes: their side arrays one after the other (one tensor map covers them)
+    const bool boxes_ok = a.bs.count == 1 || a.bs.w == (size_t)a.nx * a.ny * a.nz * 8;
+    if (a.w == nullptr || (reinterpret_cast<uintptr_t>(a.w) & 15) != 0 || a.b1_src != a.ub || !boxes_ok)
         return false;
     if (a.nx % 32 != 0 || !(a.nx / 32 == 2 || a.nx / 32 == 4 || a.nx / 32 == 8))
         return false;
@@ -472,9 +474,11 @@ static cudaError_t launch_ad6(const AdvectArgs& a, int K, cudaStream_t s)
     b.K = K;
     CUtensorMap wmap{};
     if constexpr (SW) {
-        if (a.bs.count != 1)
+        // rows of C cells of every box's side array (contiguous: bs.w is one box's array)
+        const uint64_t cells = (uint64_t)a.nx * a.ny * a.nz;
+        if (a.bs.count != 1 && a.bs.w != cells * 8)
             return cudaErrorInvalidValue;
-        e = encode_map_2d(&wmap, a.w, 2 * C, (uint64_t)a.nx * a.ny * a.nz / C, 32,
+        e = encode_map_2d(&wmap, a.w, 2 * C, cells / C * (uint64_t)a.bs.count, 32,
                           C == 8 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
         if (e != cudaSuccess)
             return e;
@@ -807,9 +811,23 @@ static int tail_slabs_ok(int nx, int ny, int nz, int kcount)
     return (plan_advect6(a, aligned, p6) && kcount % p6.K == 0) ? 1 : 0;
 }
 
+static int batch_side_ok(int n, int boxes)
+{
+    const bool aligned = ((size_t)n * 5 * sizeof(R)) % 16 == 0 && ((size_t)n * 3 * sizeof(R)) % 16 == 0;
+    if (!kV2 || boxes < 1 || plan_fluidx(n, n, aligned).C == 0)  // the x-sweep fluidx writes it
+        return 0;
+    AdvectArgs a{};  // any 16-byte aligned address stands in for the buffers
+    a.nx = a.ny = a.nz = n;
+    a.ub = a.b1_src = a.w = reinterpret_cast<const void*>(uintptr_t(256));
+    a.bs.count = boxes;
+    a.bs.w = (size_t)n * n * n * 8;
+    A6Plan p6;
+    return plan_advect6(a, aligned, p6) ? 1 : 0;
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
                                sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w, transpose_writes_w,
-                               sweep_writes_w, tail_slabs_ok};
+                               sweep_writes_w, tail_slabs_ok, batch_side_ok};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

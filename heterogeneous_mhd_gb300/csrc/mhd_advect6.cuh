@@ -93,8 +93,9 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
             if (r < J + 2) {
                 int j = j0 - 1 + r;
                 j = (j < 0) ? j + ny : (j >= ny ? j - ny : j);
-                if constexpr (SW)  // rows of C cells: 32 per pencil
-                    tma_load_2d(Us + s * USL + r * UR, &wmap, 0, (pp * ny + j) * 32, &full[s]);
+                if constexpr (SW)  // rows of C cells: 32 per pencil; the boxes' side arrays are contiguous
+                    tma_load_2d(Us + s * USL + r * UR, &wmap, 0, (((int)blockIdx.z * nz + pp) * ny + j) * 32,
+                                &full[s]);
                 else
                     tma_load_1d(Us + s * USL + r * UR, ws + ((size_t)pp * ny + j) * UR, UR * 4, &full[s]);
             } else {

@@ -35,6 +35,8 @@ struct SizeClass {
     int cfl_nparts = 0;     // partials per box currently held
     size_t ustride = 0;     // bytes between consecutive boxes' u (256-byte aligned)
     size_t bstride = 0;
+    void* W = nullptr;      // (rho, m_x) side arrays of the boxes, one after the other (FP32; only
+                            // classes whose x-sweep advectbyzx reads it, KernelSet::batch_side_ok)
     int knobs[TUNE_COUNT];  // launch-shape knobs of this class's launches (-1: the global setting)
     SizeClass() { std::fill(knobs, knobs + TUNE_COUNT, -1); }
     size_t cells() const { return (size_t)n * n * n; }
@@ -97,6 +99,7 @@ static BoxStrides strides(const mhd_batch* b, const SizeClass& c)
     s.u = c.ustride;
     s.b = c.bstride;
     s.dt = 4 * (size_t)b->elem;
+    s.w = c.W ? c.cells() * 8 : 0;
     s.count = (int)c.boxes.size();
     return s;
 }
@@ -115,6 +118,7 @@ extern "C" MHD_API int mhd_batch_destroy(mhd_batch* b)
         }
         cudaFree(c.clock);
         cudaFree(c.part);
+        cudaFree(c.W);
     }
     cudaFree(b->err_dev);
     if (b->stream)
@@ -170,6 +174,8 @@ extern "C" MHD_API int mhd_batch_create(mhd_batch** out, int nboxes, const int* 
             if (st == MHD_OK)
                 st = cu(cudaMalloc(&c.B[v], m * c.bstride));
         }
+        if (st == MHD_OK && b->elem == 4 && b->ks->batch_side_ok(c.n, (int)m))
+            st = cu(cudaMalloc(&c.W, m * c.cells() * 8));
         const size_t pa = (c.cells() + 255) / 256 + 1, pf = (size_t)b->ks->fluidx_parts(c.n, c.n, c.n, tma_ok(b, c.n));
         c.part_per_box = std::max(pa, pf);
         if (st == MHD_OK)
@@ -297,7 +303,14 @@ static int enqueue_step(mhd_batch* b, double cfl)
         fa.err = b->err_dev;
         fa.bs = bs;
         BTRY(cu(b->ks->cfl_finalize(fa, b->stream)));
-        auto F = [&](void* uo, const void* uu, const void* ub, void* part) {
+        // the side array (classes with c.W): written by the forward fluidx launches
+        // and the backward transposes, read by the advectbyzx after them, as in
+        // the single-box plain step
+        void* const Wf = (c.W && b->ks->fluidx_writes_w(n, n, n, tma_ok(b, n))) ? c.W : nullptr;
+        auto Wt = [&](int axis) -> void* {
+            return (c.W && b->ks->transpose_writes_w(axis, n, n, n)) ? c.W : nullptr;
+        };
+        auto F = [&](void* uo, const void* uu, const void* ub, void* part, void* w_out) {
             FluidxArgs a{};
             a.u_out = uo;
             a.uu = uu;
@@ -308,10 +321,11 @@ static int enqueue_step(mhd_batch* b, double cfl)
             a.cfl_part = part;
             a.err = b->err_dev;
             a.bs = bs;
+            a.w_out = w_out;
             b->launches++;
             return cu(b->ks->fluidx(a, b->stream));
         };
-        auto A = [&](void* bo, const void* b1, const void* uu, const void* ub) {
+        auto A = [&](void* bo, const void* b1, const void* uu, const void* ub, const void* w) {
             AdvectArgs a{};
             a.b_out = bo;
             a.b1_src = b1;
@@ -321,32 +335,36 @@ static int enqueue_step(mhd_batch* b, double cfl)
             a.dt_ptr = dt;
             a.err = b->err_dev;
             a.bs = bs;
+            a.w = w;
             b->launches++;
             return cu(b->ks->advect(a, b->stream));
         };
-        auto T = [&](int axis, void* uo, void* bo, const void* uu, const void* ub) {
+        auto T = [&](int axis, void* uo, void* bo, const void* uu, const void* ub, void* w_out) {
             TransposeArgs a{uo, bo, uu, ub, n, n, n, axis};
             a.bs = bs;
+            a.w_out = w_out;
             b->launches++;
             return cu(b->ks->transpose(a, b->stream));
         };
         b->launches++;
-        BTRY(F(U1, U0, B0, nullptr));
-        BTRY(A(B1, B0, U1, B0));
-        BTRY(T(1, U0, B0, U1, B1));
-        BTRY(F(U1, U0, B0, nullptr));
-        BTRY(A(B1, B0, U1, B0));
-        BTRY(T(2, U0, B0, U1, B1));
-        BTRY(F(U1, U0, B0, nullptr));
-        BTRY(A(B1, B0, U1, B0));
-        BTRY(A(B0, B1, U1, B1));
-        BTRY(F(U0, U1, B0, nullptr));
-        BTRY(T(2, U1, B1, U0, B0));
-        BTRY(A(B0, B1, U1, B1));
-        BTRY(F(U0, U1, B0, nullptr));
-        BTRY(T(1, U1, B1, U0, B0));
-        BTRY(A(B0, B1, U1, B1));
-        BTRY(F(U0, U1, B0, c.part));  // with the CFL partials of the next step
+        BTRY(F(U1, U0, B0, nullptr, Wf));
+        BTRY(A(B1, B0, U1, B0, Wf));
+        BTRY(T(1, U0, B0, U1, B1, nullptr));
+        BTRY(F(U1, U0, B0, nullptr, Wf));
+        BTRY(A(B1, B0, U1, B0, Wf));
+        BTRY(T(2, U0, B0, U1, B1, nullptr));
+        BTRY(F(U1, U0, B0, nullptr, Wf));
+        BTRY(A(B1, B0, U1, B0, Wf));
+        BTRY(A(B0, B1, U1, B1, Wf));
+        BTRY(F(U0, U1, B0, nullptr, nullptr));
+        void* W2 = Wt(2);
+        BTRY(T(2, U1, B1, U0, B0, W2));
+        BTRY(A(B0, B1, U1, B1, W2));
+        BTRY(F(U0, U1, B0, nullptr, nullptr));
+        void* W1 = Wt(1);
+        BTRY(T(1, U1, B1, U0, B0, W1));
+        BTRY(A(B0, B1, U1, B1, W1));
+        BTRY(F(U0, U1, B0, c.part, nullptr));  // with the CFL partials of the next step
         c.cfl_nparts = b->ks->fluidx_parts(n, n, n, tma_ok(b, n));
     }
     return MHD_OK;

@@ -37,6 +37,10 @@ struct KernelSet {
     // the x-sweep advectbyzx with the side array and the x-sweep fluidx) take
     // ranges of kcount planes along z (FluidxArgs/AdvectArgs::kbeg, kcount)
     int (*tail_slabs_ok)(int nx, int ny, int nz, int kcount);
+    // nonzero if a batch size class of `boxes` cubes of edge n uses the (rho, m_x)
+    // side array: its x-sweep advectbyzx is the warp-per-pencil kernel, which
+    // reads it (the boxes' arrays one after the other)
+    int (*batch_side_ok)(int n, int boxes);
 };
 
 const KernelSet* kernels_f32_fast();

@@ -193,3 +193,24 @@ def test_batch_per_edge_launch_shapes(mhd, cuda):
         for i in range(len(cfg)):
             u, b = bt.get_box(i)
             assert bitwise_equal(u, want[i][0]) and bitwise_equal(b, want[i][1]), i
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_batch_side_array_class_equals_single_box(exact, mhd, cuda):
+    """A class of 128^3 boxes runs the plain step with the (rho, m_x) side
+    array and the warp-per-pencil advectbyzx over all its boxes in one launch
+    (one tensor map over the boxes' side arrays): each box bit for bit the
+    single-box step, which uses the same kernels on one box."""
+    cfg = mhd.batch_config(4, seed=21, edges=(128, 64))
+    for x, n in zip(cfg, (128, 128, 64, 128)):
+        x["n"] = n
+    bt, ics = make_batch(mhd, cfg, exact)
+    with bt:
+        bt.step(2)
+        bt.sync()
+        for i, box in enumerate(cfg):
+            u, b = bt.get_box(i)
+            t, dt = bt.time(i)
+            su, sb, st, sdt = single(mhd, *ics[i], box["n"], 2, exact)
+            assert bitwise_equal(u, su) and bitwise_equal(b, sb), (i, box["n"])
+            assert t == st and dt == sdt, (i, t, st)
