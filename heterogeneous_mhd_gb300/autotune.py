@@ -134,8 +134,9 @@ def tune(n: int = 256, steps: int = 3, verbose: bool = False, save: bool = True)
 
 def batch_candidates(n: int):
     """Launch shapes to try for the boxes of edge n of a batch: the fluidx CTA
-    width and the marching advectbyzx (the batch's kernel; the others need
-    the side array or one box)."""
+    width and the marching advectbyzx (the planner's kernel for classes
+    without the side array; classes with it, edges 96, 128 and 256, run the
+    warp-per-pencil kernel, against which the marching shapes are timed)."""
     out = [{}]
     out += [{"fluidx.threads": t} for t in (128, 256)]
     t = n // 4

@@ -423,11 +423,12 @@ static cudaError_t advect_x4(const AdvectArgs& a, const A4Plan& p, cudaStream_t 
 }
 
 // Warp-per-pencil marching kernel (FP32, the x sweep with the side array,
-// b(1) read in place, one box): pencils of n = 32 C cells (C = 2, 4, 8), J
-// pencils per CTA (2, or 4 by advect.J), K planes per CTA (the largest that
-// gives >= 4 waves, or advect.K).  The planner's choice for pencils of 128
-// and 256 cells (at 256^3 it measured 134 against 184 us for the marching
-// kernel), and by advect.kernel = 6 for 64.
+// b(1) read in place; several boxes when their side arrays are contiguous):
+// pencils of n = 32 C cells (C = 2, 3, 4, 8), J pencils per CTA (2, or 4 by
+// advect.J), K planes per CTA (the largest that gives >= 4 waves, or
+// advect.K).  The planner's choice for pencils of 96, 128 and 256 cells (at
+// 256^3 it measured 134 against 184 us for the marching kernel), and by
+// advect.kernel = 6 for 64.
 struct A6Plan {
     int C, J, K;
 };
@@ -435,13 +436,13 @@ struct A6Plan {
 static bool plan_advect6(const AdvectArgs& a, bool aligned, A6Plan& p)
 {
     const int kn = tune_value(TUNE_ADVECT_KERNEL);
-    if (!kV2 || !aligned || a.axis != 0 || !(kn == 6 || (kn == 0 && (a.nx == 128 || a.nx == 256))))
+    if (!kV2 || !aligned || a.axis != 0 || !(kn == 6 || (kn == 0 && (a.nx == 96 || a.nx == 128 || a.nx == 256))))
         return false;
     // several boxes: their side arrays one after the other (one tensor map covers them)
     const bool boxes_ok = a.bs.count == 1 || a.bs.w == (size_t)a.nx * a.ny * a.nz * 8;
     if (a.w == nullptr || (reinterpret_cast<uintptr_t>(a.w) & 15) != 0 || a.b1_src != a.ub || !boxes_ok)
         return false;
-    if (a.nx % 32 != 0 || !(a.nx / 32 == 2 || a.nx / 32 == 4 || a.nx / 32 == 8))
+    if (a.nx % 32 != 0 || !(a.nx / 32 == 2 || a.nx / 32 == 3 || a.nx / 32 == 4 || a.nx / 32 == 8))
         return false;
     p.C = a.nx / 32;
     const int jt = tune_value(TUNE_ADVECT_J);
@@ -495,6 +496,8 @@ static cudaError_t advect_x6(const AdvectArgs& a, const A6Plan& p, cudaStream_t 
     case 84: return launch_ad6<8, 4>(a, p.K, s);
     case 42: return launch_ad6<4, 2>(a, p.K, s);
     case 44: return launch_ad6<4, 4>(a, p.K, s);
+    case 32: return launch_ad6<3, 2>(a, p.K, s);
+    case 34: return launch_ad6<3, 4>(a, p.K, s);
     case 22: return launch_ad6<2, 2>(a, p.K, s);
     case 24: return launch_ad6<2, 4>(a, p.K, s);
     }

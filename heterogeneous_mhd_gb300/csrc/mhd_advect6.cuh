@@ -23,7 +23,8 @@
 // plane k+1 during step k (the B row's upper plane, the next A row's face
 // velocity, and b(1), b(2) of the next plane, kept in registers), so a slot
 // is free again after one step.  The output pencil is written from
-// registers with 16-byte stores.
+// registers (16-byte stores for C = 4, 8; 3 C words apart for C = 3, so
+// 4-byte stores there).
 //
 // SW: the side-array pencils arrive by 2-D tensor copies whose rows are the
 // lanes' C cells (8 C bytes) with the shared-memory swizzle of that row

@@ -197,12 +197,13 @@ def test_batch_per_edge_launch_shapes(mhd, cuda):
 
 @pytest.mark.parametrize("exact", [False, True])
 def test_batch_side_array_class_equals_single_box(exact, mhd, cuda):
-    """A class of 128^3 boxes runs the plain step with the (rho, m_x) side
-    array and the warp-per-pencil advectbyzx over all its boxes in one launch
-    (one tensor map over the boxes' side arrays): each box bit for bit the
+    """Classes of 128^3 and 96^3 boxes run the plain step with the (rho, m_x)
+    side array and the warp-per-pencil advectbyzx over all their boxes in one
+    launch (128: one tensor map over the boxes' side arrays; 96: 3 cells per
+    lane, bulk copies of the side-array pencils): each box bit for bit the
     single-box step, which uses the same kernels on one box."""
-    cfg = mhd.batch_config(4, seed=21, edges=(128, 64))
-    for x, n in zip(cfg, (128, 128, 64, 128)):
+    cfg = mhd.batch_config(6, seed=21, edges=(128, 96, 64))
+    for x, n in zip(cfg, (128, 128, 64, 128, 96, 96)):
         x["n"] = n
     bt, ics = make_batch(mhd, cfg, exact)
     with bt:

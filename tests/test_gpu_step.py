@@ -268,12 +268,14 @@ def test_x_walking_advect_step_exact(kt, ns, mhd, cuda, oracle32):
 
 @pytest.mark.parametrize("shape,knobs", [((256, 32, 32), {"advect.kernel": 6}),
                                          ((256, 32, 32), {"advect.kernel": 6, "advect.J": 2, "advect.K": 8}),
-                                         ((128, 64, 64), {"advect.kernel": 6, "advect.K": 1})])
+                                         ((128, 64, 64), {"advect.kernel": 6, "advect.K": 1}),
+                                         ((96, 48, 48), {"advect.kernel": 6}),
+                                         ((96, 32, 32), {"advect.kernel": 6, "advect.J": 4, "advect.K": 2})])
 def test_warp_pencil_advect_step_exact(shape, knobs, mhd, cuda, oracle32):
     """Strang steps with the warp-per-pencil advectbyzx forced on the x sweeps
-    (pencils of 256 and 128 cells: 8 and 4 cells per lane): EXACT bit for bit
-    against the oracle after two steps, FAST bit for bit against the default
-    launch shapes after one."""
+    (pencils of 256, 128 and 96 cells: 8, 4 and 3 cells per lane): EXACT bit
+    for bit against the oracle after two steps, FAST bit for bit against the
+    default launch shapes after one."""
     from heterogeneous_mhd_gb300 import autotune
     u0, b0 = mhd.init_vortex(*shape, seed=4, vscale=1.5)
     ref = oracle32.strang(u0, b0, *shape, 2)
