@@ -364,40 +364,67 @@ def closure_leg(seeds=(1000, 1001, 1002, 1003), fine=256, factor=4, horizons=(0.
 
 def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3, tune=True):
     """The batched workload: 256 vortex boxes of edge 32..128 with their own
-    beta, Mach and dt, FP32, one graph per step; 50 timed steps.  With
-    `tune`, the launch shapes of every size class are timed on that class
-    alone first (autotune.tune_batch) and the fastest is kept per class."""
+    beta, Mach and dt, FP32, one graph per step; 50 timed steps, in two
+    groupings of the same boxes: the work-list launches (one launch per
+    operator over every size class, the library's default) and one launch
+    per class and operator, whose launch shapes (with `tune`) are timed on
+    each class alone first (autotune.tune_batch) and the fastest kept per
+    class.  The faster grouping is the headline; both are reported."""
     cfg = mhd.batch_config(nboxes, seed=rank)
     cells = sum(x["n"] ** 3 for x in cfg)
-    bt = mhd.Batch([x["n"] for x in cfg])
-    for i, box in enumerate(cfg):
-        bt.set_box(i, *mhd.init_batch_box(box))
+    hbm, _ = peaks()
+
+    def timed(bt):
+        stream = torch.cuda.ExternalStream(bt.stream())
+        bt.step(warmup)
+        bt.sync()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = bt.launch_count()
+        ev0.record(stream)
+        bt.step(steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        bt.sync()
+        step_gbs = STEP_BYTES["plain"] * cells / (ms / steps * 1e-3) / 1e9
+        return {"ms_per_step": ms / steps, "value": cells * steps / (ms * 1e-3), "unit": "cell-updates/s",
+                "step_alg_gbs": step_gbs, "step_frac": step_gbs / hbm,
+                "gpu_launches": int(bt.launch_count() - l0)}
+
+    def loaded():
+        bt = mhd.Batch([x["n"] for x in cfg])
+        for i, box in enumerate(cfg):
+            bt.set_box(i, *mhd.init_batch_box(box))
+        return bt
+
+    bt = loaded()
+    worklist = timed(bt)
+    worklist["classes_in_worklist"] = bt.worklist_classes()
+    worklist["launches_per_step"] = worklist["gpu_launches"] / steps
+    bt.close()
+
+    bt = loaded()
+    bt.set_worklist(False)
     shapes = {}
     if tune:
         from heterogeneous_mhd_gb300 import autotune
         shapes = {str(e): {"knobs": k, "ms": round(ms, 3), "planner_ms": round(b, 3)}
                   for e, (k, ms, b) in autotune.tune_batch(bt, cfg).items()}
-    stream = torch.cuda.ExternalStream(bt.stream())
-    bt.step(warmup)
-    bt.sync()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = bt.launch_count()
-    ev0.record(stream)
-    bt.step(steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    bt.sync()
-    launches = bt.launch_count() - l0
-    hbm, _ = peaks()
-    step_gbs = STEP_BYTES["plain"] * cells / (ms / steps * 1e-3) / 1e9
+    per_class = timed(bt)
+    per_class["launches_per_step"] = per_class["gpu_launches"] / steps
+    per_class["launch_shapes_per_edge"] = shapes or "planner defaults"
+    size_classes = bt.classes()
+    bt.close()
+
+    head, grouping = (worklist, "worklist") if worklist["ms_per_step"] <= per_class["ms_per_step"] else \
+        (per_class, "per_class")
     out = {"workload": f"{nboxes} vortex boxes, edges {sorted(set(x['n'] for x in cfg))}, beta 0.1-10, "
                        f"Mach 0.2-1.0, FP32, CFL 0.7, own dt per box",
-           "boxes": nboxes, "cells": cells, "size_classes": bt.classes(), "steps": steps,
-           "ms_per_step": ms / steps, "value": cells * steps / (ms * 1e-3), "unit": "cell-updates/s",
-           "step_alg_gbs": step_gbs, "step_frac": step_gbs / hbm, "gpu_launches": int(launches),
-           "launch_shapes_per_edge": shapes or "planner defaults"}
-    bt.close()
+           "boxes": nboxes, "cells": cells, "size_classes": size_classes, "steps": steps,
+           "grouping": grouping}
+    out.update({k: head[k] for k in ("ms_per_step", "value", "unit", "step_alg_gbs", "step_frac", "gpu_launches")})
+    out["worklist"] = worklist
+    out["per_class"] = per_class
     return out
 
 

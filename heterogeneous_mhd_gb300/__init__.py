@@ -136,6 +136,8 @@ def lib(build_if_missing: bool = False) -> C.CDLL:
         "mhd_batch_launch_count": (C.c_longlong, [_vp]),
         "mhd_batch_classes": (C.c_int, [_vp]),
         "mhd_batch_tune_edge": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),
+        "mhd_batch_set_worklist": (C.c_int, [_vp, C.c_int]),
+        "mhd_batch_worklist_classes": (C.c_int, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -567,3 +569,13 @@ class Batch:
     def tune_edge(self, edge: int, key: str, value: int) -> None:
         """A launch-shape knob for the boxes of one edge only (-1: the global setting)."""
         _check(lib().mhd_batch_tune_edge(self._h, int(edge), key.encode(), int(value)), "mhd_batch_tune_edge")
+
+    def set_worklist(self, on: bool) -> None:
+        """Work-list launches (default on): the classes of edge 32, 48, 64, 96
+        and 128 step with one launch per operator over all of them; off: one
+        launch per class and operator."""
+        _check(lib().mhd_batch_set_worklist(self._h, 1 if on else 0), "mhd_batch_set_worklist")
+
+    def worklist_classes(self) -> int:
+        """Size classes that step in the work-list launches."""
+        return int(lib().mhd_batch_worklist_classes(self._h))

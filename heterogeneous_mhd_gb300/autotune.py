@@ -154,9 +154,11 @@ def batch_candidates(n: int):
 def tune_batch(bt, cfg, steps: int = 3, verbose: bool = False, min_gain: float = 0.02) -> dict:
     """Per size class of a batch (`bt`, built from the box table `cfg` of
     batch_config): time every candidate shape on a batch of that class's
-    boxes alone (the same count and initial states), and set the fastest on
-    `bt` with Batch.tune_edge when it beats the planner's shapes by more than
-    min_gain.  Returns {edge: (knobs, ms per step, ms with the planner)}."""
+    boxes alone (the same count and initial states, one launch per operator),
+    and set the fastest on `bt` with Batch.tune_edge when it beats the
+    planner's shapes by more than min_gain (a class given its own shapes
+    leaves the work-list launches).  Returns {edge: (knobs, ms per step, ms
+    with the planner)}."""
     import torch
 
     from . import Batch, init_batch_box
@@ -167,6 +169,7 @@ def tune_batch(bt, cfg, steps: int = 3, verbose: bool = False, min_gain: float =
     for edge in edges:
         boxes = [x for x in cfg if x["n"] == edge]
         with Batch([edge] * len(boxes)) as one:
+            one.set_worklist(False)  # the planner's own launches are the baseline
             for i, box in enumerate(boxes):
                 one.set_box(i, *init_batch_box(box))
             stream = torch.cuda.ExternalStream(one.stream())

@@ -12,6 +12,7 @@
 #include "mhd_advect6.cuh"
 #include "mhd_fluidx2.cuh"
 #include "mhd_launch.h"
+#include "mhd_multi.cuh"
 #include "mhd_tmap.h"
 #include "mhd_transpose2.cuh"
 #include "mhd_transpose3.cuh"
@@ -828,9 +829,195 @@ static int batch_side_ok(int n, int boxes)
     return plan_advect6(a, aligned, p6) ? 1 : 0;
 }
 
+// --------------------------------------------- work-list launches (batch)
+//
+// One launch per operator over several size classes of cubes (mhd_multi.cuh):
+// `in` holds one argument set per class (nx = ny = nz = n, the class's box
+// strides and count), in launch order.  FP32 only; the classes' edges must be
+// those multi_ok accepts, their buffers 16-byte aligned, and the advectbyzx
+// arguments must carry the class's side array (contiguous over its boxes).
+
+static int multi_ok(int n) { return (kV2 && multi_kind_of_edge(n) >= 0) ? 1 : 0; }
+
+// CFL partials per box written by the work-list fluidx (one per CTA)
+static int multi_fluidx_parts(int n)
+{
+    const int T = multi_fx_threads(n);
+    return T ? (n / (kMultiFxThreads / T)) * n : 0;
+}
+
+// the advectbyzx CTA's planes along k for a class of `count` boxes of edge n
+// (the rule of plan_advect6: the largest K <= 64 that still gives 4 waves)
+static int multi_advect_k(int n, int count)
+{
+    const int ctas = advect6_min_ctas(kMultiAdJ);
+    int K = 1;
+    for (int k = 1; k <= n && k <= 64; k++)
+        if (n % k == 0 && (long long)(n / kMultiAdJ) * (n / k) * count >= 4LL * ctas * 152)
+            K = k;
+    return K;
+}
+
+static bool multi_args_ok(int nseg, const int* edges)
+{
+    if (!kV2 || nseg < 1 || nseg > kMaxSegs)
+        return false;
+    for (int i = 0; i < nseg; i++)
+        if (!multi_ok(edges[i]))
+            return false;
+    return true;
+}
+
+static cudaError_t fluidx_multi(const FluidxArgs* in, int nseg, cudaStream_t s)
+{
+    if constexpr (kV2) {
+        int edges[kMaxSegs];
+        for (int i = 0; i < nseg && i < kMaxSegs; i++)
+            edges[i] = in[i].nx;
+        if (!multi_args_ok(nseg, edges))
+            return cudaErrorInvalidValue;
+        static bool attr = false;
+        cudaError_t e = allow_smem(k_fluidx2_multi<R, EX>, attr, true);
+        if (e != cudaSuccess)
+            return e;
+        FluidxMulti m{};
+        long long total = 0;
+        size_t smem = 0;
+        for (int i = 0; i < nseg; i++) {
+            const int n = in[i].nx, T = multi_fx_threads(n), P = kMultiFxThreads / T;
+            m.a[i] = in[i];
+            m.a[i].P = P;
+            m.a[i].use_tma = 1;
+            m.g[i] = SegGrid{(int)total, n / P, n, multi_kind_of_edge(n)};
+            total += (long long)(n / P) * n * in[i].bs.count;
+            const size_t sm = fluidx2_smem_elems(n, P) * sizeof(R);
+            smem = sm > smem ? sm : smem;
+        }
+        m.nseg = nseg;
+        if (total <= 0 || total >= (1LL << 31))
+            return cudaErrorInvalidValue;
+        k_fluidx2_multi<R, EX><<<(unsigned)total, kMultiFxThreads, smem, s>>>(m);
+        return cudaGetLastError();
+    } else {
+        (void)in, (void)nseg, (void)s;
+        return cudaErrorNotSupported;
+    }
+}
+
+static cudaError_t advect_multi(const AdvectArgs* in, int nseg, cudaStream_t s)
+{
+    if constexpr (kV2) {
+        int edges[kMaxSegs];
+        for (int i = 0; i < nseg && i < kMaxSegs; i++)
+            edges[i] = in[i].nx;
+        if (!multi_args_ok(nseg, edges))
+            return cudaErrorInvalidValue;
+        static bool attr = false;
+        cudaError_t e = allow_smem(k_advect6_multi<EX>, attr, true);
+        if (e != cudaSuccess)
+            return e;
+        AdvectMulti m{};
+        long long total = 0;
+        size_t smem = 0;
+        for (int i = 0; i < nseg; i++) {
+            const AdvectArgs& a = in[i];
+            const int n = a.nx, kind = multi_kind_of_edge(n);
+            const uint64_t cells = (uint64_t)n * n * n;
+            const uintptr_t al = reinterpret_cast<uintptr_t>(a.b_out) | reinterpret_cast<uintptr_t>(a.b1_src) |
+                                 reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub) |
+                                 reinterpret_cast<uintptr_t>(a.w);
+            if (!a.w || (al & 15) != 0 || a.b1_src != a.ub || a.axis != 0 || a.kcount != 0 || a.kbeg != 0 ||
+                (a.bs.count != 1 && a.bs.w != cells * 8))
+                return cudaErrorInvalidValue;
+            const int K = multi_advect_k(n, a.bs.count);
+            m.a[i] = a;
+            m.a[i].P = kMultiAdJ;
+            m.a[i].K = K;
+            if (kind == MAD_4_32) {  // 4 cells per lane: swizzled side-array rows, one map over the boxes
+                e = encode_map_2d(&m.wmap[i], a.w, 8, cells / 4 * (uint64_t)a.bs.count, 32,
+                                  CU_TENSOR_MAP_SWIZZLE_32B);
+                if (e != cudaSuccess)
+                    return e;
+            }
+            m.g[i] = SegGrid{(int)total, n / kMultiAdJ, n / K, kind};
+            total += (long long)(n / kMultiAdJ) * (n / K) * a.bs.count;
+            const size_t sm = advect6_smem_bytes(n, kMultiAdJ);
+            smem = sm > smem ? sm : smem;
+        }
+        m.nseg = nseg;
+        if (total <= 0 || total >= (1LL << 31))
+            return cudaErrorInvalidValue;
+        k_advect6_multi<EX><<<(unsigned)total, advect6_threads(kMultiAdJ), smem, s>>>(m);
+        return cudaGetLastError();
+    } else {
+        (void)in, (void)nseg, (void)s;
+        return cudaErrorNotSupported;
+    }
+}
+
+static cudaError_t transpose_multi(const TransposeArgs* in, int nseg, cudaStream_t s)
+{
+    if constexpr (kV2) {
+        int edges[kMaxSegs];
+        for (int i = 0; i < nseg && i < kMaxSegs; i++)
+            edges[i] = in[i].nx;
+        if (!multi_args_ok(nseg, edges))
+            return cudaErrorInvalidValue;
+        const int axis = in[0].axis;
+        TransposeMulti m{};
+        long long total = 0;
+        for (int i = 0; i < nseg; i++) {
+            const TransposeArgs& a = in[i];
+            const uintptr_t al = reinterpret_cast<uintptr_t>(a.u_out) | reinterpret_cast<uintptr_t>(a.b_out) |
+                                 reinterpret_cast<uintptr_t>(a.uu) | reinterpret_cast<uintptr_t>(a.ub) |
+                                 reinterpret_cast<uintptr_t>(a.w_out);
+            if (a.axis != axis || (axis != 1 && axis != 2) || (al & 15) != 0)
+                return cudaErrorInvalidValue;
+            const int n = a.nx;
+            const int kind = (n % kT3 == 0) ? 0 : 1;
+            const int E = kind ? TTile<float>::E : kT3;
+            const int g = (n + E - 1) / E;
+            m.a[i] = a;
+            m.g[i] = SegGrid{(int)total, g, g, kind};
+            total += (long long)g * g * n * a.bs.count;
+        }
+        m.nseg = nseg;
+        if (total <= 0 || total >= (1LL << 31))
+            return cudaErrorInvalidValue;
+        if (axis == 1)
+            k_transpose_multi<1><<<(unsigned)total, 256, kMultiTransposeSmem, s>>>(m);
+        else
+            k_transpose_multi<2><<<(unsigned)total, 256, kMultiTransposeSmem, s>>>(m);
+        return cudaGetLastError();
+    } else {
+        (void)in, (void)nseg, (void)s;
+        return cudaErrorNotSupported;
+    }
+}
+
+static cudaError_t finalize_multi(const CflFinalizeArgs* in, int nseg, cudaStream_t s)
+{
+    if (nseg < 1 || nseg > kMaxSegs)
+        return cudaErrorInvalidValue;
+    FinalizeMulti m{};
+    long long total = 0;
+    for (int i = 0; i < nseg; i++) {
+        m.a[i] = in[i];
+        m.a[i].scratch = nullptr;
+        if (i > 0)
+            m.a[i].nsteps = nullptr;  // counted once per launch (box 0 of the first class)
+        m.g[i] = SegGrid{(int)total, in[i].bs.count, 1, 0};
+        total += in[i].bs.count;
+    }
+    m.nseg = nseg;
+    k_cfl_finalize_multi<R, EX><<<(unsigned)total, 1024, 0, s>>>(m);
+    return cudaGetLastError();
+}
+
 static const KernelSet kSet = {(int)sizeof(R), EX ? 1 : 0, fluidx, advect, transpose, calcfl, cfl_finalize, divb,
                                sizeof(CflPart<R>), fluidx_parts, fused_ok, fluidx_writes_w, transpose_writes_w,
-                               sweep_writes_w, tail_slabs_ok, batch_side_ok};
+                               sweep_writes_w, tail_slabs_ok, batch_side_ok, multi_ok, multi_fluidx_parts,
+                               fluidx_multi, advect_multi, transpose_multi, finalize_multi};
 
 }  // namespace MHD_SET_NAME
 }  // namespace mhd

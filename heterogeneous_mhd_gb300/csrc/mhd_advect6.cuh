@@ -50,13 +50,19 @@ __host__ __device__ inline size_t advect6_smem_bytes(int n, int J)
 
 __host__ __device__ constexpr int advect6_min_ctas(int J) { return J <= 2 ? 5 : (J <= 4 ? 3 : 2); }
 
-template <bool EX, int C, int J, bool SW = false>
-__global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
-    k_advect6(AdvectArgs a, const __grid_constant__ CUtensorMap wmap)
+// The kernel body for a CTA at block coordinates `blk` of its size class's
+// grid (HwBlock in k_advect6, VBlock in the work-list launch over several
+// classes, mhd_multi.cuh).  T = 32: a pencil of 32 C cells per warp.  T = 16
+// (short pencils of a work-list launch, 16 C cells): lanes 16..31 of a warp
+// repeat the work of lanes 0..15 on the same pencil (the group shuffles stay
+// inside each half) and store nothing.
+template <bool EX, int C, int J, bool SW, int T, typename B>
+__device__ __forceinline__ void advect6_body(AdvectArgs a, const CUtensorMap& wmap, const B& blk)
 {
     static_assert(!SW || C == 4 || C == 8, "swizzled rows of 32 or 64 bytes");
-    select_box(a, blockIdx.z);
-    constexpr int T = 32, n = C * T;
+    static_assert(T == 32 || (T == 16 && !SW), "16 or 32 cell lanes per warp");
+    select_box(a, blk.z());
+    constexpr int n = C * T;
     constexpr int UR = 2 * n, BR = 3 * n;  // floats of one staged pencil
     constexpr int USL = (J + 2) * UR, BSL = (J + 1) * BR;
     extern __shared__ __align__(16) unsigned char a6_raw[];
@@ -70,10 +76,12 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
     __shared__ uint64_t full[2];
 
     const int ny = a.ny, nz = a.nz, K = a.K;
-    const int j0 = blockIdx.x * J, k0 = a.kbeg + blockIdx.y * K;
+    const int j0 = blk.x() * J, k0 = a.kbeg + blk.y() * K;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const bool halo = (w == J);
     const Group<float, T> g(tid);
+    const int cl = g.t;               // the lane's place along the pencil (lane, for T = 32)
+    const bool owner = (lane < T);    // lanes that write shared and global memory
     const float dt = load_dt<float>(a.dt_ptr, a.dt_val);
     const float* ws = static_cast<const float*>(a.w);
     const float* ub = static_cast<const float*>(a.ub);
@@ -95,7 +103,7 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
                 int j = j0 - 1 + r;
                 j = (j < 0) ? j + ny : (j >= ny ? j - ny : j);
                 if constexpr (SW)  // rows of C cells: 32 per pencil; the boxes' side arrays are contiguous
-                    tma_load_2d(Us + s * USL + r * UR, &wmap, 0, (((int)blockIdx.z * nz + pp) * ny + j) * 32,
+                    tma_load_2d(Us + s * USL + r * UR, &wmap, 0, ((blk.z() * nz + pp) * ny + j) * 32,
                                 &full[s]);
                 else
                     tma_load_1d(Us + s * USL + r * UR, ws + ((size_t)pp * ny + j) * UR, UR * 4, &full[s]);
@@ -110,9 +118,9 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
     // this lane's C cells of side-array pencil r (0 = j0-1) / b pencil r (0 = j0) of a slot
     auto u_read = [&](int s, int r, float (&rho)[C], float (&mx)[C]) {
         float t[2 * C];
-        const float* row = Us + s * USL + r * UR + lane * 2 * C;
+        const float* row = Us + s * USL + r * UR + cl * 2 * C;
         if constexpr (SW) {
-            const int x = (C == 8) ? ((lane >> 1) & 3) : ((lane >> 2) & 1);
+            const int x = (C == 8) ? ((cl >> 1) & 3) : ((cl >> 2) & 1);
 #pragma unroll
             for (int q = 0; q < C / 2; q++) {
                 const float4 v = *reinterpret_cast<const float4*>(row + 4 * (q ^ x));
@@ -130,7 +138,7 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
             mx[m] = t[2 * m + 1];
         }
     };
-    auto b_read = [&](int s, int r, float (&bb)[3 * C]) { lds_chunk<float, 3 * C>(Bs + s * BSL + r * BR + lane * 3 * C, bb); };
+    auto b_read = [&](int s, int r, float (&bb)[3 * C]) { lds_chunk<float, 3 * C>(Bs + s * BSL + r * BR + cl * 3 * C, bb); };
     // face velocity between a lower and a current pencil (C/advectbyzxA1.c:34, C/advectbyzxB1.c:34)
     auto face = [&](const float (&rl)[C], const float (&ml)[C], const float (&rc)[C], const float (&mc)[C],
                     float (&v)[C]) {
@@ -195,7 +203,8 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
         // ---- A row (j, k) from the carried inputs
         float FA[C], bA[C];
         tvdb_row<float, EX, C, T>(g, vA, b2c, dt, nullptr, FA, bA);
-        sts_chunk<float, C>(fax + w * n + lane * C, FA);
+        if (owner)
+            sts_chunk<float, C>(fax + w * n + cl * C, FA);
         // ---- plane k+1: B row (j, k+1) and the next A row's inputs
         wait_plane(k + 1);
         const int r = halo ? J : w;
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
         // ---- combine and store pencil (j, k)
         if (!halo) {
             float fa1[C];
-            lds_chunk<float, C>(fax + (w + 1) * n + lane * C, fa1);
+            lds_chunk<float, C>(fax + (w + 1) * n + cl * C, fa1);
             float out[3 * C];
 #pragma unroll
             for (int m = 0; m < C; m++) {
@@ -237,8 +246,9 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
                 out[3 * m + BJ] = bA[m];
                 out[3 * m + BK] = b3c[m];
             }
-            const size_t cell0 = ((size_t)(k % nz) * ny + j0 + w) * n + lane * C;
-            stg_chunk<float, 3 * C>(bo + cell0 * 3, out);
+            const size_t cell0 = ((size_t)(k % nz) * ny + j0 + w) * n + cl * C;
+            if (owner)
+                stg_chunk<float, 3 * C>(bo + cell0 * 3, out);
         }
         // ---- carries for plane k+1
 #pragma unroll
@@ -251,6 +261,13 @@ __global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
             b3c[m] = b3n[m];
         }
     }
+}
+
+template <bool EX, int C, int J, bool SW = false>
+__global__ void __launch_bounds__((J + 1) * 32, advect6_min_ctas(J))
+    k_advect6(AdvectArgs a, const __grid_constant__ CUtensorMap wmap)
+{
+    advect6_body<EX, C, J, SW, 32>(a, wmap, HwBlock{});
 }
 
 }  // namespace mhd

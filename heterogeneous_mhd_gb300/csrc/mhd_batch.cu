@@ -3,11 +3,16 @@
 // edge 32..128).
 //
 // The boxes are grouped by edge length.  Each size class keeps its boxes'
-// states contiguous (ping-pong pairs like the single-box context), so every
-// operator of the Strang step (C/mhd.c:62-118) is one launch per class with
-// the box index in blockIdx.z (BoxStrides in mhd_kernels.cuh); each box has
-// its own CFL partials, clock and dt.  The whole step of every class is
-// captured into one CUDA graph.
+// states contiguous (ping-pong pairs like the single-box context); each box
+// has its own CFL partials, clock and dt.  The FP32 classes of edge 32, 48,
+// 64, 96 and 128 (up to eight classes) step together by work-list launches:
+// one launch per operator of the Strang step (C/mhd.c:62-118) walks the
+// (class, box, tile) list of all of them (mhd_multi.cuh), 17 launches per
+// step for the whole group.  Every other class, and every class given its own
+// launch shapes (mhd_batch_tune_edge) or all classes when the work list is
+// switched off (mhd_batch_set_worklist), takes one launch per operator with
+// the box index in blockIdx.z (BoxStrides in mhd_kernels.cuh).  The whole
+// step of every class is captured into one CUDA graph.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -38,7 +43,16 @@ struct SizeClass {
     void* W = nullptr;      // (rho, m_x) side arrays of the boxes, one after the other (FP32; only
                             // classes whose x-sweep advectbyzx reads it, KernelSet::batch_side_ok)
     int knobs[TUNE_COUNT];  // launch-shape knobs of this class's launches (-1: the global setting)
+    bool multi = false;     // steps in the work-list launches (assign_worklist)
+    bool side = false;      // its own launches use W (KernelSet::batch_side_ok)
     SizeClass() { std::fill(knobs, knobs + TUNE_COUNT, -1); }
+    bool own_shapes() const
+    {
+        for (int k = 0; k < TUNE_COUNT; k++)
+            if (knobs[k] >= 0)
+                return true;
+        return false;
+    }
     size_t cells() const { return (size_t)n * n * n; }
 };
 
@@ -80,6 +94,7 @@ struct mhd_batch {
     long long gtune = -1;
     int glaunches = 0;
     long long launches = 0;
+    bool worklist = true;  // eligible classes step in work-list launches
 };
 
 static int cu(cudaError_t e) { return e == cudaSuccess ? MHD_OK : (e == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA); }
@@ -92,6 +107,36 @@ static int cu(cudaError_t e) { return e == cudaSuccess ? MHD_OK : (e == cudaErro
     } while (0)
 
 static bool tma_ok(const mhd_batch* b, int n) { return ((size_t)n * 5 * b->elem) % 16 == 0 && ((size_t)n * 3 * b->elem) % 16 == 0; }
+
+// a class that can step in the work-list launches (its launch shapes are then
+// those of mhd_multi.cuh, so a class given its own shapes keeps its own launches)
+static bool worklist_ok(const mhd_batch* b, const SizeClass& c)
+{
+    return b->worklist && b->elem == 4 && b->ks->multi_ok(c.n) && tma_ok(b, c.n) && c.W && !c.own_shapes();
+}
+
+// Marks the classes of the work-list group: the eligible ones, at most
+// kMaxSegs of them (the largest by cells when there are more).
+static void assign_worklist(mhd_batch* b)
+{
+    std::vector<int> ok;
+    for (int i = 0; i < (int)b->cls.size(); i++) {
+        b->cls[i].multi = false;
+        if (worklist_ok(b, b->cls[i]))
+            ok.push_back(i);
+    }
+    std::stable_sort(ok.begin(), ok.end(), [&](int x, int y) {
+        return b->cls[x].cells() * b->cls[x].boxes.size() > b->cls[y].cells() * b->cls[y].boxes.size();
+    });
+    for (int k = 0; k < (int)ok.size() && k < kMaxSegs; k++)
+        b->cls[ok[k]].multi = true;
+}
+
+// CFL partials per box that the step's last fluidx writes for a class
+static int fluidx_parts_of(const mhd_batch* b, const SizeClass& c)
+{
+    return c.multi ? b->ks->multi_fluidx_parts(c.n) : b->ks->fluidx_parts(c.n, c.n, c.n, tma_ok(b, c.n));
+}
 
 static BoxStrides strides(const mhd_batch* b, const SizeClass& c)
 {
@@ -174,10 +219,15 @@ extern "C" MHD_API int mhd_batch_create(mhd_batch** out, int nboxes, const int* 
             if (st == MHD_OK)
                 st = cu(cudaMalloc(&c.B[v], m * c.bstride));
         }
-        if (st == MHD_OK && b->elem == 4 && b->ks->batch_side_ok(c.n, (int)m))
+        // the (rho, m_x) side array: classes whose x-sweep advectbyzx reads it, and every class
+        // that can step in the work-list launches (whose advectbyzx always reads it)
+        c.side = b->elem == 4 && b->ks->batch_side_ok(c.n, (int)m);
+        if (st == MHD_OK && (c.side || (b->elem == 4 && b->ks->multi_ok(c.n) && tma_ok(b, c.n))))
             st = cu(cudaMalloc(&c.W, m * c.cells() * 8));
         const size_t pa = (c.cells() + 255) / 256 + 1, pf = (size_t)b->ks->fluidx_parts(c.n, c.n, c.n, tma_ok(b, c.n));
         c.part_per_box = std::max(pa, pf);
+        if (b->ks->multi_ok(c.n))
+            c.part_per_box = std::max(c.part_per_box, (size_t)b->ks->multi_fluidx_parts(c.n));
         if (st == MHD_OK)
             st = cu(cudaMalloc(&c.part, m * c.part_per_box * b->ks->part_bytes));
         if (st == MHD_OK)
@@ -282,9 +332,14 @@ static int cfl_first_pass(mhd_batch* b)
 
 // One Strang step of every class (the sequence of enqueue_plain_step for a
 // single box, each launch covering all boxes of the class).
+static int enqueue_multi(mhd_batch* b, double cfl);
+
 static int enqueue_step(mhd_batch* b, double cfl)
 {
+    assign_worklist(b);
     for (auto& c : b->cls) {
+        if (c.multi)
+            continue;
         const ClassKnobs knobs(c);
         const int n = c.n;
         const BoxStrides bs = strides(b, c);
@@ -303,12 +358,12 @@ static int enqueue_step(mhd_batch* b, double cfl)
         fa.err = b->err_dev;
         fa.bs = bs;
         BTRY(cu(b->ks->cfl_finalize(fa, b->stream)));
-        // the side array (classes with c.W): written by the forward fluidx launches
+        // the side array (classes with c.side): written by the forward fluidx launches
         // and the backward transposes, read by the advectbyzx after them, as in
         // the single-box plain step
-        void* const Wf = (c.W && b->ks->fluidx_writes_w(n, n, n, tma_ok(b, n))) ? c.W : nullptr;
+        void* const Wf = (c.side && b->ks->fluidx_writes_w(n, n, n, tma_ok(b, n))) ? c.W : nullptr;
         auto Wt = [&](int axis) -> void* {
-            return (c.W && b->ks->transpose_writes_w(axis, n, n, n)) ? c.W : nullptr;
+            return (c.side && b->ks->transpose_writes_w(axis, n, n, n)) ? c.W : nullptr;
         };
         auto F = [&](void* uo, const void* uu, const void* ub, void* part, void* w_out) {
             FluidxArgs a{};
@@ -367,13 +422,125 @@ static int enqueue_step(mhd_batch* b, double cfl)
         BTRY(F(U0, U1, B0, c.part, nullptr));  // with the CFL partials of the next step
         c.cfl_nparts = b->ks->fluidx_parts(n, n, n, tma_ok(b, n));
     }
+    return enqueue_multi(b, cfl);
+}
+
+// One Strang step of the work-list group: the sequence of enqueue_step, each
+// operator one launch over every class of the group (largest first), with the
+// side array written by the forward fluidx launches and by both backward
+// transposes (both transpose kinds write it).
+static int enqueue_multi(mhd_batch* b, double cfl)
+{
+    std::vector<SizeClass*> g;
+    for (auto& c : b->cls)
+        if (c.multi)
+            g.push_back(&c);
+    if (g.empty())
+        return MHD_OK;
+    std::stable_sort(g.begin(), g.end(), [](const SizeClass* x, const SizeClass* y) {
+        return x->cells() * x->boxes.size() > y->cells() * y->boxes.size();
+    });
+    const int ns = (int)g.size();
+    const size_t dt_off = 2 * (size_t)b->elem;
+    {
+        CflFinalizeArgs fa[kMaxSegs];
+        for (int i = 0; i < ns; i++) {
+            SizeClass& c = *g[i];
+            CflFinalizeArgs x{};
+            x.part = c.part;
+            x.nparts = c.cfl_nparts;
+            x.u = c.U[0];
+            x.b = c.B[0];
+            x.nx = x.ny = x.nz = c.n;
+            x.cfl = cfl;
+            x.advance = 1;
+            x.clock = c.clock;
+            x.nsteps = b->nsteps_dev;
+            x.err = b->err_dev;
+            x.bs = strides(b, c);
+            fa[i] = x;
+        }
+        b->launches++;
+        BTRY(cu(b->ks->finalize_multi(fa, ns, b->stream)));
+    }
+    // buffer selectors: 0 / 1 = the first / second of each class's ping-pong pair
+    auto F = [&](int uo, int uu, int ub, bool part, bool w) {
+        FluidxArgs a[kMaxSegs];
+        for (int i = 0; i < ns; i++) {
+            SizeClass& c = *g[i];
+            FluidxArgs x{};
+            x.u_out = c.U[uo];
+            x.uu = c.U[uu];
+            x.ub = c.B[ub];
+            x.nx = x.ny = x.nz = c.n;
+            x.use_tma = 1;
+            x.dt_ptr = static_cast<char*>(c.clock) + dt_off;
+            x.cfl_part = part ? c.part : nullptr;
+            x.err = b->err_dev;
+            x.bs = strides(b, c);
+            x.w_out = w ? c.W : nullptr;
+            a[i] = x;
+        }
+        b->launches++;
+        return cu(b->ks->fluidx_multi(a, ns, b->stream));
+    };
+    auto A = [&](int bo, int b1, int uu, int ub) {
+        AdvectArgs a[kMaxSegs];
+        for (int i = 0; i < ns; i++) {
+            SizeClass& c = *g[i];
+            AdvectArgs x{};
+            x.b_out = c.B[bo];
+            x.b1_src = c.B[b1];
+            x.uu = c.U[uu];
+            x.ub = c.B[ub];
+            x.nx = x.ny = x.nz = c.n;
+            x.dt_ptr = static_cast<char*>(c.clock) + dt_off;
+            x.err = b->err_dev;
+            x.bs = strides(b, c);
+            x.w = c.W;
+            a[i] = x;
+        }
+        b->launches++;
+        return cu(b->ks->advect_multi(a, ns, b->stream));
+    };
+    auto T = [&](int axis, int uo, int bo, int uu, int ub, bool w) {
+        TransposeArgs a[kMaxSegs];
+        for (int i = 0; i < ns; i++) {
+            SizeClass& c = *g[i];
+            TransposeArgs x{c.U[uo], c.B[bo], c.U[uu], c.B[ub], c.n, c.n, c.n, axis};
+            x.bs = strides(b, c);
+            x.w_out = w ? c.W : nullptr;
+            a[i] = x;
+        }
+        b->launches++;
+        return cu(b->ks->transpose_multi(a, ns, b->stream));
+    };
+    BTRY(F(1, 0, 0, false, true));
+    BTRY(A(1, 0, 1, 0));
+    BTRY(T(1, 0, 0, 1, 1, false));
+    BTRY(F(1, 0, 0, false, true));
+    BTRY(A(1, 0, 1, 0));
+    BTRY(T(2, 0, 0, 1, 1, false));
+    BTRY(F(1, 0, 0, false, true));
+    BTRY(A(1, 0, 1, 0));
+    BTRY(A(0, 1, 1, 1));
+    BTRY(F(0, 1, 0, false, false));
+    BTRY(T(2, 1, 1, 0, 0, true));
+    BTRY(A(0, 1, 1, 1));
+    BTRY(F(0, 1, 0, false, false));
+    BTRY(T(1, 1, 1, 0, 0, true));
+    BTRY(A(0, 1, 1, 1));
+    BTRY(F(0, 1, 0, true, false));  // with the CFL partials of the next step
+    for (SizeClass* c : g)
+        c->cfl_nparts = b->ks->multi_fluidx_parts(c->n);
     return MHD_OK;
 }
 
-static bool steady(const mhd_batch* b)
+static bool steady(mhd_batch* b)
 {
+    assign_worklist(b);
     for (auto& c : b->cls)
-        if (c.cfl_nparts != b->ks->fluidx_parts(c.n, c.n, c.n, tma_ok(b, c.n)))
+        if (c.cfl_nparts != fluidx_parts_of(b, c))
             return false;
     return true;
 }
@@ -441,6 +608,31 @@ extern "C" MHD_API void* mhd_batch_stream(mhd_batch* b) { return b ? (void*)b->s
 extern "C" MHD_API long long mhd_batch_launch_count(mhd_batch* b) { return b ? b->launches : -1; }
 
 extern "C" MHD_API int mhd_batch_classes(mhd_batch* b) { return b ? (int)b->cls.size() : -1; }
+
+extern "C" MHD_API int mhd_batch_set_worklist(mhd_batch* b, int on)
+{
+    if (!b)
+        return MHD_ERR_ARG;
+    if (b->worklist != (on != 0)) {
+        b->worklist = (on != 0);
+        if (b->graph) {  // the step graph holds the other grouping
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+    }
+    return MHD_OK;
+}
+
+extern "C" MHD_API int mhd_batch_worklist_classes(mhd_batch* b)
+{
+    if (!b)
+        return -1;
+    assign_worklist(b);
+    int k = 0;
+    for (auto& c : b->cls)
+        k += c.multi ? 1 : 0;
+    return k;
+}
 
 extern "C" MHD_API int mhd_batch_tune_edge(mhd_batch* b, int edge, const char* key, int value)
 {

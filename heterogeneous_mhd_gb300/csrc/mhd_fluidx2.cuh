@@ -71,14 +71,16 @@ __host__ __device__ inline size_t fluidx_sweep_smem_bytes(int n)
                sizeof(float) + 128;
 }
 
-template <typename R, bool EX, int C, int T, int AX = 0>
-__global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1) : 0)
-    k_fluidx2(FluidxArgs a, const __grid_constant__ SweepMaps tm)
+// The kernel body, for a CTA at block coordinates `blk` of its size class's
+// grid (HwBlock in k_fluidx2, VBlock in the work-list launch over several
+// classes, mhd_multi.cuh).  `tm` is read by the sweeps along y and z only.
+template <typename R, bool EX, int C, int T, int AX, typename B>
+__device__ __forceinline__ void fluidx2_body(FluidxArgs a, const SweepMaps* tm, const B& blk)
 {
     static_assert(AX == 0 || (sizeof(R) == 4 && C == 4 && T <= 128), "sweeps along y, z: FP32, 4 cells, n <= 512");
     // y/z sweeps: a tensor box holds at most 256 rows, so longer pencils move in NBX boxes of BXR rows
     constexpr int NBX = (C * T + 255) / 256, BXR = C * T / NBX;
-    select_box(a, blockIdx.z, sizeof(CflPart<R>));
+    select_box(a, blk.z(), sizeof(CflPart<R>), blk.gx() * blk.gy());
     constexpr int n = C * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int P = a.P;
@@ -87,7 +89,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
     const int lp = tid / T;  // local pencil
     const Group<R, T> g(tid);
     const int i0 = g.t * C;
-    const int j0 = blockIdx.x * P, k = a.kbeg + blockIdx.y;  // k: plane along z (x sweep)
+    const int j0 = blk.x() * P, k = a.kbeg + blk.y();  // k: plane along z (x sweep)
     const int kp = (k + 1 == a.nz) ? 0 : k + 1;
     const int jn = (j0 + P == a.ny) ? 0 : j0 + P;
 
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
     } else {
         // the rows of the group (x0..x0+P-1) along the whole pencil at plane kk,
         // its b rows at plane kn, and the b of cell x0+P (periodic)
-        const int x0 = blockIdx.x * P, kk = a.kbeg + blockIdx.y;
+        const int x0 = blk.x() * P, kk = a.kbeg + blk.y();
         const int nk = (AX == 1) ? a.nz : a.ny;
         const int kn = (kk + 1 == nk) ? 0 : kk + 1;
         const int xn = (x0 + P == a.nx) ? 0 : x0 + P;
@@ -152,14 +154,14 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
 #pragma unroll
             for (int h = 0; h < NBX; h++) {  // rows h*BXR.. of the pencil
                 const int dy = (AX == 1) ? h * BXR : 0, dz = (AX == 1) ? 0 : h * BXR;
-                tma_load_3d(rows_b + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, y + dy, z + dz, &bar);
-                tma_load_3d(rows_bn + h * BXR * 4, &tm.bn_in, 3 * xn, y + dy, z + dz, &bar);
-                tma_load_3d(rows_bk + h * BXR * 3 * kSweepP, &tm.b_in, 3 * x0, yk + dy, zk + dz, &bar);
+                tma_load_3d(rows_b + h * BXR * 3 * kSweepP, &tm->b_in, 3 * x0, y + dy, z + dz, &bar);
+                tma_load_3d(rows_bn + h * BXR * 4, &tm->bn_in, 3 * xn, y + dy, z + dz, &bar);
+                tma_load_3d(rows_bk + h * BXR * 3 * kSweepP, &tm->b_in, 3 * x0, yk + dy, zk + dz, &bar);
             }
 #pragma unroll
             for (int h = 0; h < NBX; h++) {
                 const int dy = (AX == 1) ? h * BXR : 0, dz = (AX == 1) ? 0 : h * BXR;
-                tma_load_3d(rows_u + h * BXR * 5 * kSweepP, &tm.u_in, 5 * x0, y + dy, z + dz, &bar_u);
+                tma_load_3d(rows_u + h * BXR * 5 * kSweepP, &tm->u_in, 5 * x0, y + dy, z + dz, &bar_u);
             }
         }
         __syncthreads();
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
                 cm = fmax(cm, red[s]);
                 lnan = max(lnan, rn[s]);
             }
-            CflPart<R>* part = static_cast<CflPart<R>*>(a.cfl_part) + ((size_t)k * gridDim.x + blockIdx.x);
+            CflPart<R>* part = static_cast<CflPart<R>*>(a.cfl_part) + ((size_t)k * blk.gx() + blk.x());
             part->cmax = cm;
             part->last_nan = lnan;
         }
@@ -534,18 +536,25 @@ __global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1)
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
-            const int x0 = blockIdx.x * P, kk = a.kbeg + blockIdx.y;
+            const int x0 = blk.x() * P, kk = a.kbeg + blk.y();
 #pragma unroll
             for (int h = 0; h < NBX; h++) {
                 const int py = (AX == 1) ? h * BXR : kk, pz = (AX == 1) ? kk : h * BXR;
-                tma_store_3d(&tm.u_out, 5 * x0, py, pz, rows_u + h * BXR * 5 * kSweepP);
+                tma_store_3d(&tm->u_out, 5 * x0, py, pz, rows_u + h * BXR * 5 * kSweepP);
                 if (wc)
-                    tma_store_3d(&tm.w_out, 2 * x0, py, pz, rows_w + h * BXR * 2 * kSweepP);
+                    tma_store_3d(&tm->w_out, 2 * x0, py, pz, rows_w + h * BXR * 2 * kSweepP);
             }
             tma_store_commit();
             tma_store_wait_read();  // the CTA may leave once its buffers are read
         }
     }
+}
+
+template <typename R, bool EX, int C, int T, int AX = 0>
+__global__ void __launch_bounds__(AX ? kSweepP * T : 256, AX ? (T <= 64 ? 3 : 1) : 0)
+    k_fluidx2(FluidxArgs a, const __grid_constant__ SweepMaps tm)
+{
+    fluidx2_body<R, EX, C, T, AX>(a, &tm, HwBlock{});
 }
 
 }  // namespace mhd

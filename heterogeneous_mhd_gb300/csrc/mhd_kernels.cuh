@@ -26,6 +26,9 @@ struct BoxStrides {
     int count = 1;  // boxes in the launch (the launchers' grid z extent)
 };
 
+// size classes in one work-list launch (mhd_multi.cuh)
+constexpr int kMaxSegs = 8;
+
 template <typename P>
 __device__ __forceinline__ P* box_ptr(P* p, size_t stride, int box)
 {
@@ -82,15 +85,37 @@ struct TransposeArgs {
     void* w_out;          // optional (FP32 tiled kernel): (rho, m_x) of the output, 2 values per cell
 };
 
+// Coordinates of a CTA in the grid of its size class.  HwBlock reads the
+// hardware registers (a launch over one class); VBlock holds the coordinates
+// that a work-list launch over several classes (mhd_multi.cuh) derived from
+// the CTA's position in it.  Kernel bodies take either, so the one-class
+// kernels compile to the same code as before.
+struct HwBlock {
+    __device__ __forceinline__ int x() const { return (int)blockIdx.x; }
+    __device__ __forceinline__ int y() const { return (int)blockIdx.y; }
+    __device__ __forceinline__ int z() const { return (int)blockIdx.z; }
+    __device__ __forceinline__ int gx() const { return (int)gridDim.x; }
+    __device__ __forceinline__ int gy() const { return (int)gridDim.y; }
+};
+
+struct VBlock {
+    int bx, by, bz, ngx, ngy;
+    __device__ __forceinline__ int x() const { return bx; }
+    __device__ __forceinline__ int y() const { return by; }
+    __device__ __forceinline__ int z() const { return bz; }
+    __device__ __forceinline__ int gx() const { return ngx; }
+    __device__ __forceinline__ int gy() const { return ngy; }
+};
+
 // Offset every array of a launch to box `box` (the per-CTA partials of the
-// CFL epilogue too: `parts` per box).
-__device__ __forceinline__ void select_box(FluidxArgs& a, int box, size_t part_bytes)
+// CFL epilogue too: `ctas` partials per box, one per CTA of a box's grid).
+__device__ __forceinline__ void select_box(FluidxArgs& a, int box, size_t part_bytes, int ctas)
 {
     a.u_out = box_ptr(a.u_out, a.bs.u, box);
     a.uu = box_ptr(a.uu, a.bs.u, box);
     a.ub = box_ptr(a.ub, a.bs.b, box);
     a.dt_ptr = box_ptr(a.dt_ptr, a.bs.dt, box);
-    a.cfl_part = box_ptr(a.cfl_part, part_bytes * gridDim.x * gridDim.y, box);
+    a.cfl_part = box_ptr(a.cfl_part, part_bytes * (size_t)ctas, box);
     a.w_out = box_ptr(a.w_out, a.bs.w, box);
 }
 
@@ -214,7 +239,7 @@ __host__ __device__ inline size_t fluidx_smem_elems(int n, int P)
 template <typename R, bool EX>
 __global__ void __launch_bounds__(512) k_fluidx(FluidxArgs a)
 {
-    select_box(a, blockIdx.z, sizeof(CflPart<R>));
+    select_box(a, blockIdx.z, sizeof(CflPart<R>), gridDim.x * gridDim.y);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = a.nx, P = a.P;
     const int np = n * P;
@@ -607,34 +632,47 @@ struct TTile {
 // transpose12 (C/transpose12.c:7-47) and transpose13 (C/transpose13.c:9-62):
 // out(a, ., i) = in(i, ., a) with the component permutation of each.  A CTA
 // moves a 32x32 tile of cells through shared memory so both the reads (rows
-// of x) and the writes (rows of the swapped axis) are contiguous.
+// of x) and the writes (rows of the swapped axis) are contiguous.  Tiles at
+// the edges of grids that are not multiples of 32 are partial.
+//
+// The body stages into su [kTT][kTT*5+1] and sb [kTT][kTT*3+1] and takes the
+// CTA's block coordinates `blk` (HwBlock and static arrays in k_transpose,
+// VBlock and dynamic shared memory in the work-list launch over several size
+// classes, mhd_multi.cuh).  With w_out (FP32) it also writes the first two
+// components of the output cells, the (rho, m_x) side array.
 template <typename R>
-__global__ void __launch_bounds__(256) k_transpose(TransposeArgs a)
+__host__ __device__ constexpr size_t transpose_smem_bytes()
+{
+    return (size_t)TTile<R>::E * (TTile<R>::E * 8 + 2) * sizeof(R);
+}
+
+template <typename R, typename B>
+__device__ __forceinline__ void transpose_body(TransposeArgs a, R* su, R* sb, const B& blk)
 {
     constexpr int kTT = TTile<R>::E;
-    __shared__ R su[kTT][kTT * 5 + 1];
-    __shared__ R sb[kTT][kTT * 3 + 1];
+    constexpr int SU = kTT * 5 + 1, SB = kTT * 3 + 1;  // padded row strides
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int na = (a.axis == 1) ? ny : nz;  // extent of the swapped axis
     const int nbz = (a.axis == 1) ? nz : ny;  // extent of the untouched axis
-    const int i0 = blockIdx.x * kTT, a0 = blockIdx.y * kTT, z = blockIdx.z % nbz;
-    select_box(a, blockIdx.z / nbz);
+    const int i0 = blk.x() * kTT, a0 = blk.y() * kTT, z = blk.z() % nbz;
+    select_box(a, blk.z() / nbz);
     const int ti = min(kTT, nx - i0), ta = min(kTT, na - a0);
     const R* uu = static_cast<const R*>(a.uu);
     const R* ub = static_cast<const R*>(a.ub);
     R* uo = static_cast<R*>(a.u_out);
     R* bo = static_cast<R*>(a.b_out);
+    R* wo = static_cast<R*>(a.w_out);
 
     // input cell (i, a, z) for axis 1 is (i, j=a, k=z); for axis 2 it is (i, j=z, k=a)
     const size_t rstride = (a.axis == 1) ? (size_t)nx : (size_t)nx * ny;  // cells between rows of a
     const size_t cin0 = (a.axis == 1) ? (((size_t)z * ny + a0) * nx + i0) : (((size_t)a0 * ny + z) * nx + i0);
     for (int e = threadIdx.x; e < ta * ti * 5; e += blockDim.x) {
         const int r = e / (ti * 5), c = e - r * (ti * 5);
-        su[r][c] = uu[(cin0 + r * rstride) * 5 + c];
+        su[r * SU + c] = uu[(cin0 + r * rstride) * 5 + c];
     }
     for (int e = threadIdx.x; e < ta * ti * 3; e += blockDim.x) {
         const int r = e / (ti * 3), c = e - r * (ti * 3);
-        sb[r][c] = ub[(cin0 + r * rstride) * 3 + c];
+        sb[r * SB + c] = ub[(cin0 + r * rstride) * 3 + c];
     }
     __syncthreads();
     // output: axis 1 -> dims (ny,nx,nz), cell (a, i, z); axis 2 -> dims (nz,ny,nx), cell (a, z, i)
@@ -645,14 +683,30 @@ __global__ void __launch_bounds__(256) k_transpose(TransposeArgs a)
         for (int e = threadIdx.x; e < ta * 5; e += blockDim.x) {
             const int aa = e / 5, c = e - aa * 5;
             const int src = (a.axis == 1) ? perm_u<1>(c) : perm_u<2>(c);
-            uo[cout * 5 + e] = su[aa][r * 5 + src];
+            uo[cout * 5 + e] = su[aa * SU + r * 5 + src];
         }
         for (int e = threadIdx.x; e < ta * 3; e += blockDim.x) {
             const int aa = e / 3, c = e - aa * 3;
             const int src = (a.axis == 1) ? perm_b<1>(c) : perm_b<2>(c);
-            bo[cout * 3 + e] = sb[aa][r * 3 + src];
+            bo[cout * 3 + e] = sb[aa * SB + r * 3 + src];
+        }
+        if (wo) {
+            for (int e = threadIdx.x; e < ta * 2; e += blockDim.x) {
+                const int aa = e / 2, c = e - aa * 2;
+                const int src = (a.axis == 1) ? perm_u<1>(c) : perm_u<2>(c);
+                wo[cout * 2 + e] = su[aa * SU + r * 5 + src];
+            }
         }
     }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_transpose(TransposeArgs a)
+{
+    constexpr int kTT = TTile<R>::E;
+    __shared__ R su[kTT * (kTT * 5 + 1)];
+    __shared__ R sb[kTT * (kTT * 3 + 1)];
+    transpose_body<R>(a, su, sb, HwBlock{});
 }
 
 // copy_matrix (C/copy_matrix.c:9-38) as a vectorised device copy.
@@ -763,14 +817,16 @@ __global__ void __launch_bounds__(256) k_cfl_reduce(const CflPart<R>* __restrict
     }
 }
 
-template <typename R, bool EX>
-__global__ void __launch_bounds__(1024) k_cfl_finalize(CflFinalizeArgs a)
+// The kernel body for the CTA of box blk.x() (HwBlock in k_cfl_finalize,
+// VBlock in the work-list launch over several size classes, mhd_multi.cuh).
+template <typename R, bool EX, typename B>
+__device__ __forceinline__ void cfl_finalize_body(CflFinalizeArgs a, const B& blk)
 {
     using W = wide_t<R, EX>;
     __shared__ R rm[32];
     __shared__ int rn[32];
-    // batched: one CTA per box (blockIdx.x), each with its own partials, state and clock
-    const int box = blockIdx.x;
+    // batched: one CTA per box (blk.x()), each with its own partials, state and clock
+    const int box = blk.x();
     a.u = box_ptr(a.u, a.bs.u, box);
     a.b = box_ptr(a.b, a.bs.b, box);
     a.clock = box_ptr(a.clock, a.bs.dt, box);
@@ -862,6 +918,12 @@ __global__ void __launch_bounds__(1024) k_cfl_finalize(CflFinalizeArgs a)
                 *a.nsteps += 1;
         }
     }
+}
+
+template <typename R, bool EX>
+__global__ void __launch_bounds__(1024) k_cfl_finalize(CflFinalizeArgs a)
+{
+    cfl_finalize_body<R, EX>(a, HwBlock{});
 }
 
 // Max |div B| (staggered stencil, periodic): per-CTA partial maxima.

@@ -41,6 +41,16 @@ struct KernelSet {
     // side array: its x-sweep advectbyzx is the warp-per-pencil kernel, which
     // reads it (the boxes' arrays one after the other)
     int (*batch_side_ok)(int n, int boxes);
+    // Work-list launches over several size classes of cubes (mhd_multi.cuh):
+    // nonzero if a class of edge n can join one (FP32, edges 32, 48, 64, 96,
+    // 128), the CFL partials per box its fluidx writes, and one launch of an
+    // operator over `nseg` classes (one argument set per class, launch order).
+    int (*multi_ok)(int n);
+    int (*multi_fluidx_parts)(int n);
+    cudaError_t (*fluidx_multi)(const FluidxArgs* a, int nseg, cudaStream_t);
+    cudaError_t (*advect_multi)(const AdvectArgs* a, int nseg, cudaStream_t);
+    cudaError_t (*transpose_multi)(const TransposeArgs* a, int nseg, cudaStream_t);
+    cudaError_t (*finalize_multi)(const CflFinalizeArgs* a, int nseg, cudaStream_t);
 };
 
 const KernelSet* kernels_f32_fast();

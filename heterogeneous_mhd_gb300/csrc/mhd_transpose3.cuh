@@ -18,16 +18,22 @@ constexpr int kT3 = 32;
 constexpr int kT3U = 168;  // u row stride (words): 672 bytes, a multiple of 16
 constexpr int kT3B = 100;  // b row stride (words): 400 bytes
 
-template <int AXIS>
-__global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
+// shared memory of one tile (bytes): u rows, b rows (16-byte aligned)
+constexpr size_t kT3SmemBytes = (size_t)kT3 * (kT3U + kT3B) * sizeof(float);
+
+// The kernel body for a CTA at block coordinates `blk` of its size class's
+// grid, staging into su [kT3][kT3U] and sb [kT3][kT3B] (16-byte aligned):
+// HwBlock and static arrays in k_transpose3, VBlock and dynamic shared memory
+// in the work-list launch over several classes (mhd_multi.cuh).
+template <int AXIS, typename B>
+__device__ __forceinline__ void transpose3_body(TransposeArgs a, float* __restrict__ su, float* __restrict__ sb,
+                                                const B& blk)
 {
-    __shared__ __align__(16) float su[kT3 * kT3U];
-    __shared__ __align__(16) float sb[kT3 * kT3B];
     __shared__ uint64_t bar;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int nbz = (AXIS == 1) ? nz : ny;  // extent of the untouched axis
-    const int i0 = blockIdx.x * kT3, a0 = blockIdx.y * kT3, z = blockIdx.z % nbz;
-    select_box(a, blockIdx.z / nbz);
+    const int i0 = blk.x() * kT3, a0 = blk.y() * kT3, z = blk.z() % nbz;
+    select_box(a, blk.z() / nbz);
     const float* uu = static_cast<const float*>(a.uu);
     const float* ub = static_cast<const float*>(a.ub);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -87,6 +93,14 @@ __global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
                 wo[cout * 2 + lane + 32 * q] = su[sw_off[q] + 5 * i];
         }
     }
+}
+
+template <int AXIS>
+__global__ void __launch_bounds__(256) k_transpose3(TransposeArgs a)
+{
+    __shared__ __align__(16) float su[kT3 * kT3U];
+    __shared__ __align__(16) float sb[kT3 * kT3B];
+    transpose3_body<AXIS>(a, su, sb, HwBlock{});
 }
 
 }  // namespace mhd

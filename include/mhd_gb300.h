@@ -255,6 +255,18 @@ MHD_API int mhd_batch_classes(mhd_batch *batch);
  * of one edge only; -1 returns that knob to the global setting.  No
  * counterpart in the reference (see mhd_batch_create). */
 MHD_API int mhd_batch_tune_edge(mhd_batch *batch, int edge, const char *key, int value);
+/* Work-list launches (on by default): the FP32 classes of edge 32, 48, 64, 96
+ * and 128 (up to eight classes, the largest by cells when there are more) step
+ * together, each operator of the step one launch that walks the (class, box,
+ * tile) list of all of them: 17 launches per step for the whole group instead
+ * of 17 per class.  A class given its own launch shapes by
+ * mhd_batch_tune_edge keeps its own launches.  Off: one launch per class and
+ * operator.  The results are the same bit for bit either way.
+ * mhd_batch_worklist_classes returns how many classes the work list holds.
+ * No counterpart in the reference, whose driver runs one box per process
+ * (C/mhd.c:18-128). */
+MHD_API int mhd_batch_set_worklist(mhd_batch *batch, int on);
+MHD_API int mhd_batch_worklist_classes(mhd_batch *batch);
 
 /* ------------------------------------------------- initial conditions (host) */
 

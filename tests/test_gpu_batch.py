@@ -1,5 +1,7 @@
 """Batched boxes (mhd_batch_*): many independent cubes of uneven edge, each
-with its own dt, stepped together with one launch per size class per operator.
+with its own dt, stepped together: the classes of edge 32, 48, 64, 96 and 128
+by work-list launches (one launch per operator over all of them), every other
+class with one launch per size class per operator.
 
 Each box of a batch must take exactly the steps a single-box context takes on
 it: bit for bit against mhd_step for both arithmetic policies, and bit for bit
@@ -79,7 +81,10 @@ def test_batch_boxes_keep_own_dt_and_graph_launches(mhd, cuda):
         c0 = bt.launch_count()
         bt.step(3)
         bt.sync()
-        assert bt.launch_count() - c0 == 3 * 17 * ncls  # 16 operators + the dt finalize per class
+        # 16 operators + the dt finalize: once for the work-list group, once per other class
+        wl = bt.worklist_classes()
+        assert wl == ncls  # the default edges all step in the work list
+        assert bt.launch_count() - c0 == 3 * 17 * ((1 if wl else 0) + ncls - wl)
         dts = [bt.time(i)[1] for i in range(len(cfg))]
         assert all(np.isfinite(dts)) and min(dts) > 0
         assert len(set(dts)) > 1  # beta and Mach differ per box, so does dt
@@ -128,6 +133,7 @@ def test_batch_x_walking_advect_exact_vs_oracle(mhd, cuda, oracle32):
         autotune.apply({"advect.kernel": 4, "advect.xk": 4})
         bt, ics = make_batch(mhd, cfg, exact=True)
         with bt:
+            bt.set_worklist(False)  # the global knobs shape the per-class launches only
             bt.step(3)
             bt.sync()
             for i, box in enumerate(cfg):
@@ -195,18 +201,21 @@ def test_batch_per_edge_launch_shapes(mhd, cuda):
             assert bitwise_equal(u, want[i][0]) and bitwise_equal(b, want[i][1]), i
 
 
+@pytest.mark.parametrize("worklist", [False, True])
 @pytest.mark.parametrize("exact", [False, True])
-def test_batch_side_array_class_equals_single_box(exact, mhd, cuda):
+def test_batch_side_array_class_equals_single_box(exact, worklist, mhd, cuda):
     """Classes of 128^3 and 96^3 boxes run the plain step with the (rho, m_x)
     side array and the warp-per-pencil advectbyzx over all their boxes in one
     launch (128: one tensor map over the boxes' side arrays; 96: 3 cells per
-    lane, bulk copies of the side-array pencils): each box bit for bit the
-    single-box step, which uses the same kernels on one box."""
+    lane, bulk copies of the side-array pencils), per class or in the work
+    list: each box bit for bit the single-box step, which uses the same
+    kernels on one box."""
     cfg = mhd.batch_config(6, seed=21, edges=(128, 96, 64))
     for x, n in zip(cfg, (128, 128, 64, 128, 96, 96)):
         x["n"] = n
     bt, ics = make_batch(mhd, cfg, exact)
     with bt:
+        bt.set_worklist(worklist)
         bt.step(2)
         bt.sync()
         for i, box in enumerate(cfg):
@@ -215,3 +224,65 @@ def test_batch_side_array_class_equals_single_box(exact, mhd, cuda):
             su, sb, st, sdt = single(mhd, *ics[i], box["n"], 2, exact)
             assert bitwise_equal(u, su) and bitwise_equal(b, sb), (i, box["n"])
             assert t == st and dt == sdt, (i, t, st)
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_worklist_equals_per_class_launches(exact, mhd, cuda):
+    """The work-list launches (one launch per operator over the classes of
+    edge 32, 48, 64, 96 and 128; a class of edge 40 keeps its own launches)
+    give every box the bits of one launch per class and operator, on the same
+    initial states, after three steps; the whole work-list step is 17
+    launches."""
+    cfg = mhd.batch_config(9, seed=29)
+    for x, n in zip(cfg, (128, 96, 64, 48, 32, 32, 48, 40, 64)):
+        x["n"] = n
+    ref, ics = make_batch(mhd, cfg, exact)
+    with ref:
+        ref.set_worklist(False)
+        assert ref.worklist_classes() == 0
+        ref.step(3)
+        ref.sync()
+        want = [ref.get_box(i) for i in range(len(cfg))]
+        want_t = [ref.time(i) for i in range(len(cfg))]
+    bt, _ = make_batch(mhd, cfg, exact)
+    with bt:
+        assert bt.worklist_classes() == 5 and bt.classes() == 6
+        bt.step(2)
+        c0 = bt.launch_count()
+        bt.step(1)
+        bt.sync()
+        assert bt.launch_count() - c0 == 17 + 17  # the work list + the class of edge 40
+        for i in range(len(cfg)):
+            u, b = bt.get_box(i)
+            assert bitwise_equal(u, want[i][0]) and bitwise_equal(b, want[i][1]), (i, cfg[i]["n"])
+            assert bt.time(i) == want_t[i], i
+
+
+def test_worklist_switch_and_own_shapes(mhd, cuda):
+    """Switching the work list off and on between steps, and a class leaving it
+    when given its own launch shapes, change only the launches: the FAST boxes
+    stay bit for bit those of an uninterrupted work-list run."""
+    cfg = mhd.batch_config(6, seed=31, edges=(32, 64, 96))
+    ref, ics = make_batch(mhd, cfg, exact=False)
+    with ref:
+        ref.step(4)
+        ref.sync()
+        want = [ref.get_box(i) for i in range(len(cfg))]
+    bt, _ = make_batch(mhd, cfg, exact=False)
+    with bt:
+        nw = bt.worklist_classes()
+        bt.step(1)
+        bt.set_worklist(False)
+        bt.step(1)
+        bt.set_worklist(True)
+        edge = cfg[0]["n"]
+        bt.tune_edge(edge, "advect.K", 4)
+        assert bt.worklist_classes() == nw - 1
+        bt.step(1)
+        bt.tune_edge(edge, "advect.K", -1)
+        assert bt.worklist_classes() == nw
+        bt.step(1)
+        bt.sync()
+        for i in range(len(cfg)):
+            u, b = bt.get_box(i)
+            assert bitwise_equal(u, want[i][0]) and bitwise_equal(b, want[i][1]), i
