@@ -391,11 +391,14 @@ def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3, tune=True):
                 "step_alg_gbs": step_gbs, "step_frac": step_gbs / hbm,
                 "gpu_launches": int(bt.launch_count() - l0)}
 
-    def loaded():
-        bt = mhd.Batch([x["n"] for x in cfg])
-        for i, box in enumerate(cfg):
+    def loaded_boxes(boxes):
+        bt = mhd.Batch([x["n"] for x in boxes])
+        for i, box in enumerate(boxes):
             bt.set_box(i, *mhd.init_batch_box(box))
         return bt
+
+    def loaded():
+        return loaded_boxes(cfg)
 
     bt = loaded()
     worklist = timed(bt)
@@ -416,6 +419,19 @@ def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3, tune=True):
     size_classes = bt.classes()
     bt.close()
 
+    # each size class alone, in both groupings (the planner's launch shapes), after the
+    # whole batch
+    per_edge = {}
+    for e in sorted({x["n"] for x in cfg}):
+        boxes = [x for x in cfg if x["n"] == e]
+        row = {"boxes": len(boxes)}
+        for name, on in (("worklist_ms", True), ("per_class_ms", False)):
+            one = loaded_boxes(boxes)
+            one.set_worklist(on)
+            row[name] = round(timed(one)["ms_per_step"], 4)
+            one.close()
+        per_edge[str(e)] = row
+
     head, grouping = (worklist, "worklist") if worklist["ms_per_step"] <= per_class["ms_per_step"] else \
         (per_class, "per_class")
     out = {"workload": f"{nboxes} vortex boxes, edges {sorted(set(x['n'] for x in cfg))}, beta 0.1-10, "
@@ -425,6 +441,7 @@ def batch_leg(mhd, torch, rank, nboxes=256, steps=50, warmup=3, tune=True):
     out.update({k: head[k] for k in ("ms_per_step", "value", "unit", "step_alg_gbs", "step_frac", "gpu_launches")})
     out["worklist"] = worklist
     out["per_class"] = per_class
+    out["each_class_alone"] = per_edge
     return out
 
 
