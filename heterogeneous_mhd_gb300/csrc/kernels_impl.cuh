@@ -704,6 +704,14 @@ static cudaError_t transpose(const TransposeArgs& a, cudaStream_t s)
                 k_transpose3<2><<<grid, 256, 0, s>>>(a);
             return cudaGetLastError();
         }
+        if (a.nx % 16 == 0 && na % 16 == 0 && (al & 15) == 0) {  // bulk-TMA tiles of 16 cells
+            dim3 grid(a.nx / 16, na / 16, nb * a.bs.count);
+            if (a.axis == 1)
+                k_transpose3<1, 16><<<grid, 256, 0, s>>>(a);
+            else
+                k_transpose3<2, 16><<<grid, 256, 0, s>>>(a);
+            return cudaGetLastError();
+        }
         if (a.nx % kT2 == 0 && na % kT2 == 0 && (al & 3) == 0) {
             dim3 grid(a.nx / kT2, na / kT2, nb * a.bs.count);
             if (a.axis == 1)
@@ -974,8 +982,8 @@ static cudaError_t transpose_multi(const TransposeArgs* in, int nseg, cudaStream
             if (a.axis != axis || (axis != 1 && axis != 2) || (al & 15) != 0)
                 return cudaErrorInvalidValue;
             const int n = a.nx;
-            const int kind = (n % kT3 == 0) ? 0 : 1;
-            const int E = kind ? TTile<float>::E : kT3;
+            const int kind = (n % 32 == 0) ? 0 : ((n % 16 == 0) ? 2 : 1);
+            const int E = (kind == 0) ? 32 : ((kind == 2) ? 16 : TTile<float>::E);
             const int g = (n + E - 1) / E;
             m.a[i] = a;
             m.g[i] = SegGrid{(int)total, g, g, kind};

@@ -147,8 +147,9 @@ __global__ void __launch_bounds__((kMultiAdJ + 1) * 32, 6)
     }
 }
 
-// kind 0: bulk-TMA tiles (edges that are multiples of 32), 1: the general
-// tile kernel (partial tiles); both with the side-array output
+// kind 0: bulk-TMA tiles of 32 cells (edges that are multiples of 32), 2: of
+// 16 cells (multiples of 16), 1: the general tile kernel (partial tiles); all
+// with the side-array output
 constexpr size_t kMultiTransposeSmem =
     kT3SmemBytes > transpose_smem_bytes<float>() ? kT3SmemBytes : transpose_smem_bytes<float>();
 
@@ -162,7 +163,9 @@ __global__ void __launch_bounds__(256, 6) k_transpose_multi(const __grid_constan
     const int s = multi_seg(m.g, m.nseg);
     const VBlock blk = multi_block(m.g[s]);
     if (m.g[s].kind == 0)
-        transpose3_body<AXIS>(m.a[s], sm, sm + kT3 * kT3U, blk);
+        transpose3_body<AXIS, 32>(m.a[s], sm, sm + 32 * T3Tile<32>::SU, blk);
+    else if (m.g[s].kind == 2)
+        transpose3_body<AXIS, 16>(m.a[s], sm, sm + 16 * T3Tile<16>::SU, blk);
     else
         transpose_body<float>(m.a[s], sm, sm + TTile<float>::E * (TTile<float>::E * 5 + 1), blk);
 }

@@ -68,7 +68,9 @@ def test_fast_ops_close_to_reference_golden(mhd, cuda):
                     assert rel_l2(got, ref) < FAST_OP_TOL, f"{name} {key}: {rel_l2(got, ref):.2e}"
 
 
-SHAPES = [(64, 64, 64), (48, 48, 48), (256, 8, 4), (100, 6, 5), (512, 2, 2), (96, 12, 96), (3, 5, 7), (4, 1, 1)]
+# (48, 48, 48), (80, 16, 80), (16, 48, 16): transposes in bulk-TMA tiles of 16 cells
+SHAPES = [(64, 64, 64), (48, 48, 48), (256, 8, 4), (100, 6, 5), (512, 2, 2), (96, 12, 96), (3, 5, 7), (4, 1, 1),
+          (80, 16, 80), (16, 48, 16)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
