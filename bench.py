@@ -725,6 +725,21 @@ def ncu_closure_case(args):
     torch.cuda.synchronize()
 
 
+def ncu_batch_case(args):
+    """A short run of the batch's work-list kernels for ncu captures: the
+    first 32 boxes of the batched workload's table (edges 32-128, 26 M
+    cells, 1.9 GB of states and side arrays), three work-list steps, no
+    JSON line."""
+    import heterogeneous_mhd_gb300 as mhd
+
+    cfg = mhd.batch_config(32, seed=0)
+    with mhd.Batch([x["n"] for x in cfg]) as bt:
+        for i, box in enumerate(cfg):
+            bt.set_box(i, *mhd.init_batch_box(box))
+        bt.step(3)
+        bt.sync()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -741,6 +756,7 @@ def main():
     ap.add_argument("--no-512", action="store_true", help="skip the 512^3 plain-step leg")
     ap.add_argument("--ncu-case", action="store_true", help="run the short profiling case only")
     ap.add_argument("--ncu-closure", action="store_true", help="run the short closure profiling case only")
+    ap.add_argument("--ncu-batch", action="store_true", help="run the short work-list batch profiling case only")
     ap.add_argument("--tcgen05", type=int, default=1,
                     help="--ncu-closure: 1 warp-specialised tcgen05 convolution, 2 two-buffer, 0 mma.sync")
     ap.add_argument("--knob", action="append", default=[], help="launch-shape knob key=value for --ncu-case")
@@ -750,6 +766,8 @@ def main():
         ap.error("--warmup must be >= 3")
     if args.ncu_closure:
         ncu_closure_case(args)
+    elif args.ncu_batch:
+        ncu_batch_case(args)
     elif args.ncu_case:
         ncu_case(args)
     elif args.impl == "reference":
