@@ -128,8 +128,9 @@ __global__ void __launch_bounds__(kMultiFxThreads) k_fluidx2_multi(const __grid_
 }
 
 // The bound of six CTAs per SM makes ptxas allocate 96 registers, as for the
-// 4-cell kind alone, so seven CTAs of three warps fit on an SM; without it
-// the union of the kinds took 109 registers and six CTAs (18.85 against
+// 4-cell kind alone, so six CTAs of three warps fit on an SM (registers are
+// allocated per sub-partition: five warps of 96 registers each); without it
+// the union of the kinds took 109 registers and five CTAs (18.85 against
 // 18.53 ms per step for 61 boxes of 128^3).
 template <bool EX>
 __global__ void __launch_bounds__((kMultiAdJ + 1) * 32, 6)
