@@ -3,8 +3,10 @@
 //
 // Each operator has a register-resident kernel for the common pencil lengths
 // (fluidx: n = 4T with T in {8..128} or 3T with T in {16..128}; advectbyzx:
-// n = 8T, T in {4..64} or 6T, T in {8..64}; transposes: full 32x32 tiles) and
-// a general kernel for every other shape.  FP64 uses the general kernels.
+// n = 8T, T in {4..64} or 6T, T in {8..64}; transposes: full 32x32 tiles, or
+// 16x16 tiles for edges that are multiples of 16) and a general kernel for
+// every other shape.  FP64 uses the general kernels.  The batch's work-list
+// launches (one launch per operator over several size classes) are at the end.
 #include "mhd_advect2.cuh"
 #include "mhd_advect3.cuh"
 #include "mhd_advect4.cuh"

@@ -40,8 +40,9 @@ struct SizeClass {
     int cfl_nparts = 0;     // partials per box currently held
     size_t ustride = 0;     // bytes between consecutive boxes' u (256-byte aligned)
     size_t bstride = 0;
-    void* W = nullptr;      // (rho, m_x) side arrays of the boxes, one after the other (FP32; only
-                            // classes whose x-sweep advectbyzx reads it, KernelSet::batch_side_ok)
+    void* W = nullptr;      // (rho, m_x) side arrays of the boxes, one after the other (FP32; classes
+                            // whose own x-sweep advectbyzx reads it, KernelSet::batch_side_ok, and
+                            // classes that can step in the work list, whose advectbyzx always reads it)
     int knobs[TUNE_COUNT];  // launch-shape knobs of this class's launches (-1: the global setting)
     bool multi = false;     // steps in the work-list launches (assign_worklist)
     bool side = false;      // its own launches use W (KernelSet::batch_side_ok)
@@ -330,8 +331,9 @@ static int cfl_first_pass(mhd_batch* b)
     return MHD_OK;
 }
 
-// One Strang step of every class (the sequence of enqueue_plain_step for a
-// single box, each launch covering all boxes of the class).
+// One Strang step of every class: the classes outside the work list first
+// (the sequence of enqueue_plain_step for a single box, each launch covering
+// all boxes of the class), then the work-list group (enqueue_multi).
 static int enqueue_multi(mhd_batch* b, double cfl);
 
 static int enqueue_step(mhd_batch* b, double cfl)
@@ -428,7 +430,7 @@ static int enqueue_step(mhd_batch* b, double cfl)
 // One Strang step of the work-list group: the sequence of enqueue_step, each
 // operator one launch over every class of the group (largest first), with the
 // side array written by the forward fluidx launches and by both backward
-// transposes (both transpose kinds write it).
+// transposes (every transpose kind of the work list writes it).
 static int enqueue_multi(mhd_batch* b, double cfl)
 {
     std::vector<SizeClass*> g;
