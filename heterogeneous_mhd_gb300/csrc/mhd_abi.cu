@@ -398,6 +398,7 @@ static int op_transpose(mhd_ctx* c, int axis, void* u, void* b, const void* uu, 
     if (axis == 2 && nx != nz && !(degenerate && (nx == 1 || nz == 1)))
         return MHD_ERR_ARG;
     TransposeArgs a{u, b, uu, ub, nx, ny, nz, axis};
+    a.err = c->err_dev;
     a.w_out = w_out;
     KTimer kt(c, axis == 1 ? MHD_K_TRANSPOSE12 : MHD_K_TRANSPOSE13);
     CUDA_TRY(c->ks->transpose(a, c->stream));

@@ -398,6 +398,7 @@ static int enqueue_step(mhd_batch* b, double cfl)
         };
         auto T = [&](int axis, void* uo, void* bo, const void* uu, const void* ub, void* w_out) {
             TransposeArgs a{uo, bo, uu, ub, n, n, n, axis};
+            a.err = b->err_dev;
             a.bs = bs;
             a.w_out = w_out;
             b->launches++;
@@ -510,6 +511,7 @@ static int enqueue_multi(mhd_batch* b, double cfl)
         for (int i = 0; i < ns; i++) {
             SizeClass& c = *g[i];
             TransposeArgs x{c.U[uo], c.B[bo], c.U[uu], c.B[ub], c.n, c.n, c.n, axis};
+            x.err = b->err_dev;
             x.bs = strides(b, c);
             x.w_out = w ? c.W : nullptr;
             a[i] = x;

@@ -83,6 +83,7 @@ struct TransposeArgs {
     int axis;             // 1: x<->y (transpose12), 2: x<->z (transpose13, nx == nz)
     BoxStrides bs;
     void* w_out;          // optional (FP32 tiled kernel): (rho, m_x) of the output, 2 values per cell
+    int* err = nullptr;   // optional: the bulk-TMA tile kernel sets DEVERR_TIMEOUT here when a copy never lands
 };
 
 // Coordinates of a CTA in the grid of its size class.  HwBlock reads the

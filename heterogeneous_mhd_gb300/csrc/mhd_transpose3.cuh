@@ -87,7 +87,10 @@ __device__ __forceinline__ void transpose3_body(TransposeArgs a, float* __restri
         const int f = lane + 32 * q, aa = f / 3, c = f - 3 * aa;
         sb_off[q] = (f < 3 * E) ? aa * SB + perm_b<AXIS>(c) : 0;
     }
-    mbar_wait_bounded(&bar, 0, nullptr);
+    // a copy that never lands (the wait gave up and set the error bit): the
+    // whole CTA leaves before writing from unfilled shared memory
+    if (!__syncthreads_and(mbar_wait_bounded(&bar, 0, a.err)))
+        return;
 
     float* uo = static_cast<float*>(a.u_out);
     float* bo = static_cast<float*>(a.b_out);
