@@ -87,3 +87,40 @@ def test_port_matches_reference_build_random_shapes(mhd, oracle32):
                 getattr(o, o_name)(uo, bo, nx, ny, nz, 0.1, u.copy(), b.copy())
                 outs.append((uo, bo))
             assert bitwise_equal(outs[0][0], outs[1][0]) and bitwise_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_calcfl_nan_and_inf_cells_match_reference_build(bits, mhd, oracle32, oracle64):
+    """calcfl's handling of non-finite speeds, pinned to the reference build
+    itself: max_2num (C/calcfl.c:91-101) restarts the running maximum after a
+    NaN, so a NaN in a middle cell is skipped, a NaN in the last cell makes
+    1/c NaN, and an infinite speed gives 1/c = 0.  The GPU kernels' NaN tests
+    check against this oracle (development container only)."""
+    from _oracle import Oracle, have_ref
+    if not have_ref():
+        pytest.skip("no reference build and no MHD_REF_SRC on this machine")
+    port = oracle32 if bits == 32 else oracle64
+    ref = Oracle(bits, "ref")
+    dt = np.float32 if bits == 32 else np.float64
+    nx, ny, nz = 12, 6, 5
+    nc = nx * ny * nz
+    u0, b0 = mhd.init_vortex(nx, ny, nz, seed=41, fp64=(bits == 64))
+    cases = {"middle": [(nc // 2 + 3, 0)], "last": [(nc - 1, 0)], "first": [(0, 0)],
+             "two": [(17, 0), (nc - 40, 4)], "b only": [(nc // 3, "b")], "inf": [(nc // 4, "inf")]}
+    for name, cells in cases.items():
+        u, b = u0.astype(dt).copy(), b0.astype(dt).copy()
+        for cell, comp in cells:
+            if comp == "b":
+                b[cell * 3 + 1] = np.nan
+            elif comp == "inf":
+                u[cell * 5 + 1] = np.inf
+            else:
+                u[cell * 5 + comp] = np.nan
+        got, want = port.calcfl(u, b, nx, ny, nz), ref.calcfl(u, b, nx, ny, nz)
+        assert (np.isnan(got) and np.isnan(want)) or got == want, (name, got, want)
+        if name == "last":
+            assert np.isnan(want)
+        if name in ("middle", "first", "two", "b only"):
+            assert np.isfinite(want) and want > 0, (name, want)
+        if name == "inf":
+            assert want == 0, want
