@@ -124,3 +124,46 @@ def test_calcfl_nan_and_inf_cells_match_reference_build(bits, mhd, oracle32, ora
             assert np.isfinite(want) and want > 0, (name, want)
         if name == "inf":
             assert want == 0, want
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_port_matches_reference_build_every_operator(bits, mhd, oracle32, oracle64):
+    """Every operator of the path (fluidx, advectbyzx, transpose12,
+    transpose13 where nx == nz, copy_matrix, calcfl) of the restatement
+    against oracle/_ref on fresh odd shapes, in both precisions, bit for bit
+    (development container only)."""
+    from _oracle import Oracle, have_ref
+    if not have_ref():
+        pytest.skip("no reference build and no MHD_REF_SRC on this machine")
+    port = oracle32 if bits == 32 else oracle64
+    ref = Oracle(bits, "ref")
+    dt = np.float32 if bits == 32 else np.float64
+    rng = np.random.default_rng(11 + bits)
+    shapes = [tuple(int(x) for x in rng.integers(1, 13, size=3)) for _ in range(5)] + [(9, 4, 9), (7, 7, 7)]
+    for nx, ny, nz in shapes:
+        u, b = mhd.init_vortex(nx, ny, nz, seed=int(rng.integers(1 << 30)), fp64=(bits == 64))
+        u, b = u.astype(dt), b.astype(dt)
+        outs = []
+        for o in (port, ref):
+            res = {}
+            uo, bo = np.full_like(u, 3), (b * dt(0.5)).astype(dt)
+            o.fluidx(uo, bo, nx, ny, nz, 0.05, u.copy(), b.copy())
+            res["fluidx"] = (uo, bo)
+            uo, bo = u.copy(), (b * dt(0.75)).astype(dt)
+            o.advectbyzx(uo, bo, nx, ny, nz, 0.05, u.copy(), b.copy())
+            res["advectbyzx"] = (uo, bo)
+            ut, bt = np.zeros_like(u), np.zeros_like(b)
+            o.transpose12(ut, bt, u.copy(), b.copy(), nx, ny, nz)
+            res["transpose12"] = (ut, bt)
+            if nx == nz:
+                ut, bt = np.zeros_like(u), np.zeros_like(b)
+                o.transpose13(ut, bt, u.copy(), b.copy(), nx, ny, nz)
+                res["transpose13"] = (ut, bt)
+            uc, bc = np.zeros_like(u), np.zeros_like(b)
+            o.copy_matrix(u.copy(), b.copy(), nx, ny, nz, uc, bc)
+            res["copy_matrix"] = (uc, bc)
+            res["calcfl"] = (np.array([o.calcfl(u, b, nx, ny, nz)], dtype=dt),)
+            outs.append(res)
+        for name in outs[0]:
+            for got, want in zip(outs[0][name], outs[1][name]):
+                assert bitwise_equal(got, want), (name, (nx, ny, nz), bits)
